@@ -1,0 +1,90 @@
+"""Build the tracker's shared library in-tree: ``libfrg_gb300.so`` next to this file.
+
+Every CUDA translation unit is compiled for sm_103a only
+(``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked with the
+host C++ translation unit into one C-ABI shared library (include/frg_gb300.h).
+Runs with nvcc alone (no cmake, no torch); the same recipe builds on x86 and on
+the aarch64 GPU hosts.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libfrg_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_SOURCES = ["frg_track.cu", "frg_capi.cu"]
+CXX_SOURCES = ["frg_collect.cpp"]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libfrg_gb300.so")
+    return path
+
+
+def _sources_newer_than(target: str) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps += [os.path.join(HERE, "..", "include", "frg_gb300.h"), __file__]
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
+    """Compile (if stale) and return the path of libfrg_gb300.so."""
+    if not force and not _sources_newer_than(LIB):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-I", CSRC, "-I", os.path.join(HERE, "..", "include")]
+    jobs = []
+    for src in CUDA_SOURCES:
+        obj = os.path.join(BUILD, src + ".o")
+        cmd = [cc, *ARCH, *common, "-c", os.path.join(CSRC, src), "-o", obj]
+        if ptxas_info:
+            cmd += ["-Xptxas", "-v"]
+        jobs.append((cmd, obj))
+    for src in CXX_SOURCES:
+        obj = os.path.join(BUILD, src + ".o")
+        cmd = [cc, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(HERE, "..", "include"),
+               "-c", os.path.join(CSRC, src), "-o", obj]
+        jobs.append((cmd, obj))
+
+    def run(job):
+        cmd, _ = job
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        logs = list(ex.map(run, jobs))
+    if ptxas_info or verbose:
+        for log in logs:
+            if log.strip():
+                print(log, file=sys.stderr)
+    tmp = LIB + ".tmp"
+    link = [cc, *ARCH, "-shared", "-o", tmp] + [o for _, o in jobs] + ["-lcudart"]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, ptxas_info="-v" in sys.argv, force="-f" in sys.argv)
+    print(LIB)

@@ -1,0 +1,346 @@
+// C ABI of the tracker: contexts, configuration and the tracking entry points
+// (include/frg_gb300.h). Replaces the reference driver's allocation block,
+// InitRandStates/Homotopy launches and copies back (frg.cu:201-236, :351-404).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/frg_gb300.h"
+#include "frg_kernels.h"
+#include "frg_rng.h"
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct frg_ctx {
+  int device = 0;
+  frg_config cfg;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int sm_count = 0;
+  int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each kernel mode
+  std::string err;
+  DevBuf fpm, gamma, fpm_lo, gamma_lo, task_start, queue, counters, roots, codes, yfinal, resid;
+  DevBuf handoff, handoff_list;
+};
+
+static frg_status fail(frg_ctx* ctx, frg_status s, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+static frg_status cuda_fail(frg_ctx* ctx, cudaError_t e, const char* where) {
+  return fail(ctx, FRG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define FRG_CUDA(ctx, call)                                  \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+extern "C" frg_status frg_config_default(frg_config* c) {
+  if (!c) return FRG_ERR_ARG;
+  std::memset(c, 0, sizeof(*c));
+  // htpytrack.cu:9-31
+  c->s_init = 1.0; c->s_max = 100.0; c->s_min = 1e-6; c->rk_tol = 1e-3;
+  c->caution_steps = 2;
+  c->newt_its = 10; c->newt_tol = 1e-8; c->newt_residual = 1; c->newt_attempts = 3;
+  c->sharp_its = 30; c->sharp_tol = 1e-12; c->sharp_residual = 1; c->sharp_attempts = 3;
+  c->sharp_trigger = 1e-5; c->nudge_trigger = 1e-5;
+  c->max_steps = 2000; c->max_ministeps = 3000;
+  c->patch_range = 2.0;
+  // frgkinematics.cu:7-8
+  c->start_dist = FRG_START_UNIFORM; c->start_range = 5.0;
+  // frg.cu:41
+  c->gamma_mode = FRG_GAMMA_FIXED; c->gamma_re = 0.39231132891081666; c->gamma_im = 1.0062265257923928;
+  // frgsupport.cu:7
+  c->dup_tol = 1e-6;
+  c->precision = FRG_PREC_FP64;
+  c->t_switch = 0.99;
+  c->cond_switch = 1e6;
+  c->inf_tol = 0.0;
+  c->threads_per_block = 0;
+  c->blocks_per_sm = 0;
+  c->newt_tol_lo = 1e-5;
+  return FRG_OK;
+}
+
+static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
+  if (!c) return fail(ctx, FRG_ERR_ARG, "config is NULL");
+  if (!(c->s_init > 0) || !(c->s_min > 0) || !(c->s_max >= c->s_min) || !(c->rk_tol > 0))
+    return fail(ctx, FRG_ERR_ARG, "step sizes and rk_tol must be positive with s_max >= s_min");
+  if (c->newt_its < 0 || c->sharp_its < 0 || c->newt_attempts < 1 || c->sharp_attempts < 1 ||
+      c->max_steps < 0 || c->max_ministeps < 0)
+    return fail(ctx, FRG_ERR_ARG, "iteration limits must be non-negative (attempts >= 1)");
+  if (c->start_dist != FRG_START_UNIFORM && c->start_dist != FRG_START_NORMAL)
+    return fail(ctx, FRG_ERR_ARG, "unknown start_dist");
+  if (c->gamma_mode != FRG_GAMMA_FIXED && c->gamma_mode != FRG_GAMMA_RANDOM)
+    return fail(ctx, FRG_ERR_ARG, "unknown gamma_mode");
+  if (c->precision != FRG_PREC_FP64 && c->precision != FRG_PREC_MIXED)
+    return fail(ctx, FRG_ERR_ARG, "unknown precision");
+  if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
+    return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
+  return FRG_OK;
+}
+
+extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int device) {
+  if (!out) return FRG_ERR_ARG;
+  *out = nullptr;
+  frg_ctx* ctx = new (std::nothrow) frg_ctx();
+  if (!ctx) return FRG_ERR_ALLOC;
+  frg_config def;
+  frg_config_default(&def);
+  ctx->cfg = cfg ? *cfg : def;
+  frg_status s = check_config(nullptr, &ctx->cfg);
+  if (s != FRG_OK) { delete ctx; return s; }
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  for (int m = 0; m < 3 && e == cudaSuccess; ++m) {
+    e = frg_track_occupancy(m, &ctx->blocks_per_sm[m]);
+    if (ctx->blocks_per_sm[m] < 1) ctx->blocks_per_sm[m] = 1;
+  }
+  if (e != cudaSuccess) {
+    frg_destroy(ctx);
+    return FRG_ERR_CUDA;
+  }
+  *out = ctx;
+  return FRG_OK;
+}
+
+extern "C" void frg_destroy(frg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (DevBuf* b : {&ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->task_start, &ctx->queue,
+                    &ctx->counters, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->handoff,
+                    &ctx->handoff_list})
+    b->release();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+extern "C" const char* frg_last_error(const frg_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" frg_status frg_set_config(frg_ctx* ctx, const frg_config* cfg) {
+  if (!ctx) return FRG_ERR_ARG;
+  frg_status s = check_config(ctx, cfg);
+  if (s != FRG_OK) return s;
+  ctx->cfg = *cfg;
+  return FRG_OK;
+}
+
+// gamma of task k: the configured constant (frg.cu:41) or e^{i phi}, phi uniform,
+// drawn from a stream of `seed` reserved for gammas.
+static void task_gammas(const frg_config& c, uint64_t seed, int ntasks, std::vector<cx<double>>& g) {
+  g.resize(ntasks);
+  for (int k = 0; k < ntasks; ++k) {
+    if (c.gamma_mode == FRG_GAMMA_FIXED) {
+      g[k] = cx<double>(c.gamma_re, c.gamma_im);
+    } else {
+      double phi = 6.283185307179586 * frg_uniform01(seed, 0xFFFFFFFFFFFFFFFFull - (uint64_t)k, 0);
+      g[k] = cx<double>(std::cos(phi), std::sin(phi));
+    }
+  }
+}
+
+// Shared body of frg_track / frg_track_async. Device pointers only here.
+static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntasks, const int64_t* ppt,
+                                uint64_t seed, cx<double>* d_roots, int32_t* d_codes, cx<double>* d_yfinal,
+                                double* d_resid, int64_t N, cudaStream_t st) {
+  const bool mixed = ctx->cfg.precision == FRG_PREC_MIXED;
+  std::vector<cx<double>> g;
+  task_gammas(ctx->cfg, seed, ntasks, g);
+  std::vector<cx<float>> g_lo(ntasks);
+  for (int k = 0; k < ntasks; ++k) g_lo[k] = cx<float>(g[k]);
+  std::vector<int64_t> starts(ntasks + 1, 0);
+  for (int k = 0; k < ntasks; ++k) starts[k + 1] = starts[k] + ppt[k];
+  FRG_CUDA(ctx, ctx->gamma.ensure(sizeof(cx<double>) * ntasks));
+  FRG_CUDA(ctx, ctx->gamma_lo.ensure(sizeof(cx<float>) * ntasks));
+  FRG_CUDA(ctx, ctx->fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, ctx->task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
+  FRG_CUDA(ctx, ctx->queue.ensure(sizeof(unsigned long long) * 4));
+  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 16));
+  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma.p, g.data(), sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_lo.p, g_lo.data(), sizeof(cx<float>) * ntasks, cudaMemcpyHostToDevice,
+                                st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->task_start.p, starts.data(), sizeof(int64_t) * (ntasks + 1),
+                                cudaMemcpyHostToDevice, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(ctx->queue.p, 0, sizeof(unsigned long long) * 4, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 16, st));
+  FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)ctx->fpm_lo.p, FRG_NP * ntasks, st));
+
+  frg::TrackArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.cfg = ctx->cfg;
+  a.fpm = d_fpm;
+  a.gamma = (const cx<double>*)ctx->gamma.p;
+  a.fpm_lo = (const cx<float>*)ctx->fpm_lo.p;
+  a.gamma_lo = (const cx<float>*)ctx->gamma_lo.p;
+  a.task_start = (const int64_t*)ctx->task_start.p;
+  a.ntasks = ntasks;
+  a.npaths = N;
+  a.seed = seed;
+  unsigned long long* q = (unsigned long long*)ctx->queue.p;
+  a.queue = q;
+  a.roots = d_roots;
+  a.codes = d_codes;
+  a.yfinal = d_yfinal;
+  a.resid = d_resid;
+  a.work = nullptr;
+  a.counters = (unsigned long long*)ctx->counters.p;
+  auto grid_for = [&](int mode, int64_t n) {
+    int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm : ctx->blocks_per_sm[mode];
+    int64_t grid = (int64_t)ctx->sm_count * bps;
+    int64_t need = (n + FRG_TRACK_THREADS - 1) / FRG_TRACK_THREADS;
+    if (grid > need) grid = need;
+    return (int)(grid < 1 ? 1 : grid);
+  };
+  if (!mixed) {
+    cudaError_t e = frg_launch_track(0, a, grid_for(0, N), st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64)");
+    return FRG_OK;
+  }
+  FRG_CUDA(ctx, ctx->handoff.ensure(sizeof(frg::Handoff) * (size_t)N));
+  FRG_CUDA(ctx, ctx->handoff_list.ensure(sizeof(int64_t) * (size_t)N));
+  a.handoff = (frg::Handoff*)ctx->handoff.p;
+  a.handoff_list = (int64_t*)ctx->handoff_list.p;
+  a.handoff_count = q + 2;
+  a.queue = q;
+  cudaError_t e = frg_launch_track(1, a, grid_for(1, N), st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
+  a.queue = q + 1;
+  e = frg_launch_track(2, a, grid_for(2, N), st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
+  return FRG_OK;
+}
+
+static frg_status check_track_args(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* ppt, double* roots,
+                                   int32_t* codes, int64_t* N) {
+  if (!ctx) return FRG_ERR_ARG;
+  if (ntasks < 1 || !ppt || !fpm) return fail(ctx, FRG_ERR_ARG, "need ntasks >= 1, fpm and paths_per_task");
+  int64_t n = 0;
+  for (int k = 0; k < ntasks; ++k) {
+    if (ppt[k] < 0) return fail(ctx, FRG_ERR_ARG, "paths_per_task must be non-negative");
+    n += ppt[k];
+  }
+  if (n > 0 && (!roots || !codes)) return fail(ctx, FRG_ERR_ARG, "roots and codes are required");
+  *N = n;
+  return FRG_OK;
+}
+
+extern "C" frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                                      uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
+                                      void* stream) {
+  int64_t N = 0;
+  frg_status s = check_track_args(ctx, fpm, ntasks, paths_per_task, roots, codes, &N);
+  if (s != FRG_OK) return s;
+  if (N == 0) return FRG_OK;
+  FRG_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!is_device_ptr(fpm) || !is_device_ptr(roots) || !is_device_ptr(codes) || (yfinal && !is_device_ptr(yfinal)) ||
+      (resid && !is_device_ptr(resid)))
+    return fail(ctx, FRG_ERR_ARG, "frg_track_async takes device pointers only");
+  return enqueue_track(ctx, (const cx<double>*)fpm, ntasks, paths_per_task, seed, (cx<double>*)roots, codes,
+                       (cx<double>*)yfinal, resid, N, (cudaStream_t)stream);
+}
+
+extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                                uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
+                                frg_stats* stats) {
+  auto t0 = std::chrono::steady_clock::now();
+  int64_t N = 0;
+  frg_status s = check_track_args(ctx, fpm, ntasks, paths_per_task, roots, codes, &N);
+  if (s != FRG_OK) return s;
+  if (stats) { std::memset(stats, 0, sizeof(*stats)); stats->paths = N; }
+  if (N == 0) return FRG_OK;
+  FRG_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+
+  // inputs
+  const cx<double>* d_fpm = (const cx<double>*)fpm;
+  if (!is_device_ptr(fpm)) {
+    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks));
+    FRG_CUDA(ctx, cudaMemcpyAsync(ctx->fpm.p, fpm, sizeof(cx<double>) * 30 * ntasks, cudaMemcpyHostToDevice, st));
+    d_fpm = (const cx<double>*)ctx->fpm.p;
+  }
+  // outputs: written in place when on the device, staged otherwise
+  struct Out { void* user; DevBuf* buf; size_t bytes; void* dev; bool host; };
+  Out outs[4] = {{roots, &ctx->roots, sizeof(cx<double>) * 21 * (size_t)N, nullptr, false},
+                 {codes, &ctx->codes, sizeof(int32_t) * (size_t)N, nullptr, false},
+                 {yfinal, &ctx->yfinal, sizeof(cx<double>) * 23 * (size_t)N, nullptr, false},
+                 {resid, &ctx->resid, sizeof(double) * (size_t)N, nullptr, false}};
+  for (Out& o : outs) {
+    if (!o.user) continue;
+    if (is_device_ptr(o.user)) { o.dev = o.user; }
+    else {
+      FRG_CUDA(ctx, o.buf->ensure(o.bytes));
+      o.dev = o.buf->p;
+      o.host = true;
+    }
+  }
+  FRG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  s = enqueue_track(ctx, d_fpm, ntasks, paths_per_task, seed, (cx<double>*)outs[0].dev, (int32_t*)outs[1].dev,
+                    (cx<double>*)outs[2].dev, (double*)outs[3].dev, N, st);
+  if (s != FRG_OK) return s;
+  FRG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  for (Out& o : outs)
+    if (o.user && o.host) FRG_CUDA(ctx, cudaMemcpyAsync(o.user, o.dev, o.bytes, cudaMemcpyDeviceToHost, st));
+  unsigned long long cnt[16], qv[4];
+  FRG_CUDA(ctx, cudaMemcpyAsync(cnt, ctx->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(qv, ctx->queue.p, sizeof(qv), cudaMemcpyDeviceToHost, st));
+  FRG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (stats) {
+    for (int k = 0; k < 8; ++k) stats->codes[k] = (int64_t)cnt[k];
+    stats->ivp_solves = (int64_t)cnt[8];
+    stats->newton_iters = (int64_t)cnt[9];
+    stats->steps = (int64_t)cnt[10];
+    stats->fp64_solves = (int64_t)cnt[11];
+    stats->handoffs = ctx->cfg.precision == FRG_PREC_MIXED ? (int64_t)qv[2] : 0;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats->track_ms = ms;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return FRG_OK;
+}

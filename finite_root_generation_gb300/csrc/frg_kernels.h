@@ -1,0 +1,53 @@
+// Internal interface between the C ABI (frg_capi.cu) and the tracking kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/frg_gb300.h"
+#include "frg_complex.cuh"
+
+#ifndef FRG_TRACK_THREADS
+#define FRG_TRACK_THREADS 64
+#endif
+
+namespace frg {
+
+// Saved state of a path handed from the FP32 stage to the FP64 stage: what the
+// reference's tracker carries across loop iterations (htpytrack.cu:36-77).
+struct Handoff {
+  cx<double> Yc[23], Vc[23], u[23];
+  double s;
+  uint64_t rng_index;
+  int streak, step, ministep, tstepQ, n_ivp, n_newton, reason, pad;
+};
+
+// Device-side arguments of one tracking launch. All arrays are device memory.
+struct TrackArgs {
+  frg_config cfg;
+  const cx<double>* fpm;        // ntasks x 30 target parameters
+  const cx<double>* gamma;      // ntasks
+  const cx<float>* fpm_lo;      // FP32 copies for the FP32 stage
+  const cx<float>* gamma_lo;
+  const int64_t* task_start;    // ntasks + 1 prefix sums of paths per task
+  int ntasks;
+  int64_t npaths;
+  uint64_t seed;
+  unsigned long long* queue;    // work-queue head, zeroed before launch
+  cx<double>* roots;            // npaths x 21
+  int32_t* codes;               // npaths
+  cx<double>* yfinal;           // npaths x 23, optional
+  double* resid;                // npaths, optional
+  int32_t* work;                // npaths x 3 (ivp solves, newton iterations, steps), optional
+  unsigned long long* counters; // 16: codes[8], ivp, newton, steps, -, -, fp64 solves
+  Handoff* handoff;             // npaths slots (mixed precision)
+  int64_t* handoff_list;        // ids of handed-off paths
+  unsigned long long* handoff_count;
+};
+
+}  // namespace frg
+
+// mode: 0 plain FP64, 1 FP32 stage with handoff, 2 FP64 resume of handed-off paths
+cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
+cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm);
+cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);

@@ -1,0 +1,505 @@
+// The path-tracking kernels.
+//
+// One CUDA thread tracks one path at a time and pulls the next path index from a
+// device work queue (an atomic counter) when its path ends, so the very uneven
+// path lengths (tens to thousands of steps) do not hold a whole launch back the
+// way the reference's one-path-per-thread launch does (frg.cu:25-27, :374).
+//
+// The reference's nested tracking loops (TrackPath, htpytrack.cu:83-216, with
+// DormandPrince65, rungekutta.cu:3-123, and Newton, htpysupport.cu:407-494) are
+// restated as a state machine in which every trip performs exactly one linear
+// system step -- Jacobian evaluation, row scaling, LU and solve, either a
+// predictor tangent (IVP, htpysupport.cu:237-299) or a corrector iteration -- so
+// the expensive part runs converged across the warp while the cheap control logic
+// around it diverges. The decisions, tolerances, counters and random draws are the
+// reference's, so a path ends with the reference's code and root.
+//
+// Three instantiations:
+//   MODE_PLAIN   FP64 throughout, from the start system to the root (the reference's
+//                arithmetic);
+//   MODE_LO      FP32 state and linear algebra from the start system; a path is handed
+//                to FP64 (its state saved to HBM) when t reaches t_switch, when an LU
+//                pivot ratio exceeds cond_switch, when a prediction enters the endgame
+//                (t > 1 - nudge_trigger), or when a step would fail at s_min;
+//   MODE_RESUME  FP64, continuing handed-off paths from their saved state through the
+//                endgame and sharpening.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "frg_device.cuh"
+#include "frg_kernels.h"
+
+namespace frg {
+
+// Dormand-Prince 6(5) tableau (rungekutta.cu:261-341): stage weights, error
+// weights (LTE, :318-324) and 6th-order solution weights (:334-341).
+__constant__ double c_dpA[8][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {1. / 10., 0, 0, 0, 0, 0, 0},
+    {-2. / 81., 20. / 81., 0, 0, 0, 0, 0},
+    {615. / 1372., -270. / 343., 1053. / 1372., 0, 0, 0, 0},
+    {3243. / 5500., -54. / 55., 50949. / 71500., 4998. / 17875., 0, 0, 0},
+    {-26492. / 37125., 72. / 55., 2808. / 23375., -24206. / 37125., 338. / 459., 0, 0},
+    {5561. / 2376., -35. / 11., -24117. / 31603., 899983. / 200772., -5225. / 1836., 3925. / 4056., 0},
+    {465467. / 266112., -2945. / 1232., -5610201. / 14158144., 10513573. / 3212352., -424325. / 205632.,
+     376225. / 454272., 0}};
+__constant__ double c_dpE[8] = {-13. / 2400., 0., 19683. / 618800., -2401. / 31200., 65. / 816.,
+                                -15. / 416., -521. / 5600., 1. / 10.};
+__constant__ double c_dpB[8] = {61. / 864., 0., 98415. / 321776., 16807. / 146016., 1375. / 7344.,
+                                1375. / 5408., -37. / 1120., 1. / 10.};
+
+enum Phase : int { PH_FETCH = 0, PH_TANGENT0 = 1, PH_RK = 2, PH_NEWTON = 3, PH_SHARP = 4 };
+enum Mode : int { MODE_PLAIN = 0, MODE_LO = 1, MODE_RESUME = 2 };
+
+template <typename T>
+struct PathState {
+  cx<T> Yc[NY], Vc[NY], Yn[NY], Vn[NY], YN[NY], u[NY];
+  cx<T> k[8][NY];
+  cx<T> spm[NP];
+  Rng rng;
+  int64_t id;
+  int task;
+  T s, err, scale, residual;
+  int tstepQ, streak, step, ministep, stage, attempt, it, phase, code;
+  int n_ivp, n_newton;
+};
+
+template <typename T>
+__device__ __forceinline__ void draw_patch(Rng& r, double range, cx<T>* u) {
+#pragma unroll 1
+  for (int i = 0; i < NY; ++i) {
+    double re = 2.0 * range * r.uniform() - range;
+    double im = 2.0 * range * r.uniform() - range;
+    u[i] = cx<T>(T(re), T(im));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T vnorm(const cx<T>* v, int n) {
+  T s = T(0);
+#pragma unroll 1
+  for (int i = 0; i < n; ++i) s += cnorm2(v[i]);
+  return sqrt(s);
+}
+
+// sum_{l < n} w[l] * s * k[l][e], accumulated from the last term to the first as the
+// reference's nested .add() chains do (rungekutta.cu:262-341).
+template <typename T>
+__device__ __forceinline__ cx<T> comb(const double* w, T s, const cx<T> (*k)[NY], int n, int e) {
+  cx<T> acc(T(0));
+  bool first = true;
+  for (int l = n - 1; l >= 0; --l) {
+    if (w[l] == 0.0) continue;
+    cx<T> term = (T(w[l]) * s) * k[l][e];
+    acc = first ? term : term + acc;
+    first = false;
+  }
+  return acc;
+}
+
+// Hand the path to the corrector (htpytrack.cu:135-154) or to sharpening
+// (:194-213): YN starts from the prediction Yn.
+template <typename T>
+__device__ __forceinline__ void begin_newton(PathState<T>& P, int phase) {
+#pragma unroll 1
+  for (int e = 0; e < NY; ++e) P.YN[e] = P.Yn[e];
+  P.residual = T(100);
+  P.it = 0;
+  P.phase = phase;
+}
+
+__device__ void finish_path(const TrackArgs& a, int64_t id, int task, int code, cd* Yf, const cd* fpm);
+
+// The task arrays in the working precision (FP32 copies are prepared by the host).
+template <typename T> __device__ __forceinline__ const cx<T>* task_fpm(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ const cx<double>* task_fpm<double>(const TrackArgs& a, int task) {
+  return a.fpm + (size_t)task * NP;
+}
+template <> __device__ __forceinline__ const cx<float>* task_fpm<float>(const TrackArgs& a, int task) {
+  return a.fpm_lo + (size_t)task * NP;
+}
+template <typename T> __device__ __forceinline__ cx<T> task_gamma(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ cx<double> task_gamma<double>(const TrackArgs& a, int task) {
+  return a.gamma[task];
+}
+template <> __device__ __forceinline__ cx<float> task_gamma<float>(const TrackArgs& a, int task) {
+  return a.gamma_lo[task];
+}
+
+template <typename T>
+__device__ void save_handoff(const TrackArgs& a, const PathState<T>& P, int reason) {
+  Handoff& h = a.handoff[P.id];
+#pragma unroll 1
+  for (int e = 0; e < NY; ++e) {
+    h.Yc[e] = cd(P.Yc[e]);
+    h.Vc[e] = cd(P.Vc[e]);
+    h.u[e] = cd(P.u[e]);
+  }
+  h.s = double(P.s);
+  h.rng_index = P.rng.index;
+  h.streak = P.streak; h.step = P.step; h.ministep = P.ministep; h.tstepQ = P.tstepQ;
+  h.n_ivp = P.n_ivp; h.n_newton = P.n_newton; h.reason = reason;
+  const unsigned long long slot = atomicAdd(a.handoff_count, 1ull);
+  a.handoff_list[slot] = P.id;
+}
+
+template <int MODE, typename T>
+__global__ void __launch_bounds__(FRG_TRACK_THREADS)
+track_kernel(TrackArgs a) {
+  const frg_config& c = a.cfg;
+  constexpr bool LO = (MODE == MODE_LO);
+  const T newt_tol = LO ? T(c.newt_tol_lo) : T(c.newt_tol);
+  PathState<T> P;
+  cx<T> Ye[NY], q[NP], dq[NP], F[NZ], b[NY], x[NY];
+  cx<T> M[NY * LDM];
+  P.phase = PH_FETCH;
+  unsigned long long fp64_solves = 0;
+  const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count : a.npaths;
+
+  for (;;) {
+    // ------------------------------------------------------------------ fetch
+    if (P.phase == PH_FETCH) {
+      const int64_t qi = (int64_t)atomicAdd(a.queue, 1ull);
+      if (qi >= nqueue) break;
+      const int64_t id = (MODE == MODE_RESUME) ? a.handoff_list[qi] : qi;
+      P.id = id;
+      int lo = 0, hi = a.ntasks - 1;  // task of this path
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (a.task_start[mid] <= id) lo = mid; else hi = mid - 1;
+      }
+      P.task = lo;
+      // Start system (frg.cu:54): the stream of path id; TrackPath receives the same
+      // fresh state (frg.cu:57, by value), so its draws restart at index 0.
+      P.rng.seed = a.seed; P.rng.stream = (uint64_t)id; P.rng.index = 0;
+      cd spt[NV], spm[NP];
+      generate_start(P.rng, c.start_dist, c.start_range, spt, spm);
+#pragma unroll 1
+      for (int e = 0; e < NP; ++e) P.spm[e] = cx<T>(spm[e]);
+      P.code = 0; P.stage = 0; P.attempt = 0; P.it = 0; P.residual = T(100); P.err = T(0); P.scale = T(0);
+      if (MODE == MODE_RESUME) {
+        const Handoff& h = a.handoff[id];
+#pragma unroll 1
+        for (int e = 0; e < NY; ++e) { P.Yc[e] = cx<T>(h.Yc[e]); P.Vc[e] = cx<T>(h.Vc[e]); P.u[e] = cx<T>(h.u[e]); }
+        P.s = T(h.s); P.rng.index = h.rng_index;
+        P.streak = h.streak; P.step = h.step; P.ministep = h.ministep; P.tstepQ = h.tstepQ;
+        P.n_ivp = h.n_ivp; P.n_newton = h.n_newton;
+        P.phase = PH_RK;
+      } else {
+        P.rng.index = 0;
+#pragma unroll 1
+        for (int e = 0; e < NV; ++e) P.Yc[e] = cx<T>(spt[e]);
+        P.Yc[NV] = cx<T>(T(1));
+        P.Yc[NV + 1] = cx<T>(T(0));
+        draw_patch(P.rng, c.patch_range, P.u);
+        switch_patch(P.u, P.Yc, P.Yc);
+        draw_patch(P.rng, c.patch_range, P.Vc);
+        P.s = T(c.s_init); P.tstepQ = 0; P.streak = c.caution_steps - 1; P.step = 0; P.ministep = 0;
+        P.n_ivp = 0; P.n_newton = 0;
+        P.phase = PH_TANGENT0;
+      }
+    }
+
+    // -------------------------------------------------- set up the linear step
+    const cx<T>* fpmT = task_fpm<T>(a, P.task);
+    const cx<T> gamma = task_gamma<T>(a, P.task);
+    const bool newton = (P.phase == PH_NEWTON || P.phase == PH_SHARP);
+    bool tstep = false;
+    const cx<T>* patch = P.Vc;
+    if (P.phase == PH_TANGENT0) {
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) Ye[e] = P.Yc[e];
+    } else if (P.phase == PH_RK) {
+      tstep = P.tstepQ != 0;
+      const int st = P.stage;
+      if (st == 0) {
+#pragma unroll 1
+        for (int e = 0; e < NY; ++e) Ye[e] = P.Yc[e];
+      } else {
+        patch = P.k[st - 1];
+#pragma unroll 1
+        for (int e = 0; e < NY; ++e) Ye[e] = P.Yc[e] + comb(c_dpA[st], P.s, P.k, st, e);
+      }
+    } else {
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) Ye[e] = P.YN[e];
+    }
+
+    // ------------------------------------------------------ the linear step
+    params_at<T>(Ye[NY - 1].re, P.spm, fpmT, gamma, q, dq);
+    if (MODE != MODE_LO) fp64_solves++;
+    system_rows<T>(Ye, q, dq, M, newton ? F : nullptr);
+    // row 21: the projective patch u (htpysupport.cu:139-142); row 22: the velocity patch
+#pragma unroll 1
+    for (int e = 0; e < NY; ++e) { M[21 * LDM + e] = P.u[e]; M[22 * LDM + e] = patch[e]; }
+    T hnorm = T(0), ratio;
+    if (newton) {
+      cx<T> d(T(0));
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) d = cfma(P.u[e], Ye[e], d);
+      F[NV] = d - cx<T>(T(1));
+      hnorm = vnorm(F, NZ);
+      row_scale<T>(M, NZ, F);
+#pragma unroll 1
+      for (int e = 0; e < NZ; ++e) b[e] = -F[e];
+      b[NZ] = cx<T>(T(0));
+      const T tgoal = (P.phase == PH_SHARP) ? T(1) : P.Yn[NY - 1].re;
+      ratio = lu_solve<T>(M, b, x, NZ, true, cx<T>(tgoal - Ye[NY - 1].re));
+      P.n_newton++;
+    } else {
+      row_scale<T>(M, NZ, nullptr);
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) b[e] = cx<T>(T(0));
+      b[NY - 1] = cx<T>(T(1));
+      ratio = lu_solve<T>(M, b, x, NY, false, cx<T>(T(0)));
+      // normalise the tangent (htpysupport.cu:285-296): unit length with real
+      // dt/ds, or dt = 1 when stepping in t. conj(x22)/|x22| is the reference's
+      // (cos theta, -sin theta) with theta = arg(x22).
+      cx<T> sc;
+      if (!tstep) {
+        const T ax = sqrt(cnorm2(x[NY - 1]));
+        sc = cx<T>(x[NY - 1].re, -x[NY - 1].im) * (T(1) / (ax * vnorm(x, NY)));
+      } else {
+        sc = cinv(x[NY - 1]);
+      }
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) x[e] = sc * x[e];
+      x[NY - 1].im = T(0);
+      P.n_ivp++;
+    }
+
+    // ------------------------------------------------------------- transitions
+    bool finished = false;
+    int handoff = 0;
+    const cx<T>* final_src = P.Yc;  // the reference's Yc aliases Yfinal (htpytrack.cu:46)
+    if (LO && !(ratio <= T(c.cond_switch))) {
+      handoff = 2;  // ill-conditioned (or non-finite) step: continue in FP64 from Yc
+    } else if (P.phase == PH_TANGENT0) {
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) P.Vc[e] = x[e];
+      if (c.max_steps == 0) { P.code = 1; finished = true; }
+      P.stage = 0;
+      P.phase = PH_RK;
+    } else if (P.phase == PH_RK) {
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) P.k[P.stage][e] = x[e];
+      if (++P.stage == 8) {
+        P.stage = 0;
+        // error estimate and step factor (rungekutta.cu:317-331), prediction (:333-341)
+        T es = T(0);
+#pragma unroll 1
+        for (int e = 0; e < NY; ++e) {
+          es += cnorm2(comb(c_dpE, P.s, P.k, 8, e));
+          P.Yn[e] = P.Yc[e] + comb(c_dpB, P.s, P.k, 8, e);
+          P.Vn[e] = P.k[7][e];
+        }
+        P.err = sqrt(es);
+        P.scale = (P.err > T(10e-17)) ? T(0.8) * pow(T(c.rk_tol) / P.err, T(1) / T(6)) : T(5);
+        if (P.scale > T(5)) P.scale = T(5);
+        if (P.ministep++ == c.max_ministeps) { P.code = 2; finished = true; }
+        else if (P.err <= T(c.rk_tol)) {
+          const T tn = P.Yn[NY - 1].re;
+          if (LO && tn > T(1.0 - c.nudge_trigger)) handoff = 5;  // the endgame runs in FP64
+          else if (tn <= T(1.0 - c.nudge_trigger)) { P.attempt = 0; begin_newton(P, PH_NEWTON); }
+          else if (fabs(T(1) - tn) < T(c.sharp_trigger)) { P.attempt = 0; begin_newton(P, PH_SHARP); }
+          else { P.tstepQ = 1; P.s = T(1) - P.Yc[NY - 1].re; }  // land on t = 1 (htpytrack.cu:120-123)
+        } else {
+          if (P.s <= T(c.s_min)) {
+            if (LO) handoff = 4; else { P.code = 3; finished = true; }
+          } else {
+            P.s *= P.scale;
+            if (P.s < T(c.s_min)) P.s = T(c.s_min * 0.9);
+            P.streak = 0;
+          }
+        }
+      }
+    } else {
+      // one corrector or sharpening iteration (htpysupport.cu:427-492)
+      const bool sharp = (P.phase == PH_SHARP);
+      const int max_its = sharp ? c.sharp_its : c.newt_its;
+      const T tol = sharp ? T(c.sharp_tol) : newt_tol;
+      const int restype = sharp ? c.sharp_residual : c.newt_residual;
+      bool done = false;
+      if (restype == 0 && P.it > 0) {
+        // |H| at the current point is the residual of the previous update
+        P.residual = hnorm;
+        if (!(P.it < max_its && P.residual > tol)) done = true;
+      }
+      if (!done) {
+#pragma unroll 1
+        for (int e = 0; e < NY; ++e) P.YN[e] += x[e];
+        P.it++;
+        if (restype != 0) {
+          P.residual = vnorm(x, NY);
+          if (!(P.it < max_its && P.residual > tol)) done = true;
+        }
+      }
+      if (done) {
+        if (!sharp) {
+          if (P.ministep++ == c.max_ministeps) { P.code = 2; finished = true; }
+          else if (P.residual < newt_tol) {
+            if (fabs(T(1) - P.Yn[NY - 1].re) < T(c.sharp_trigger)) { P.attempt = 0; begin_newton(P, PH_SHARP); }
+            else {
+              // accept the step (htpytrack.cu:176-183)
+#pragma unroll 1
+              for (int e = 0; e < NY; ++e) { P.Yc[e] = P.YN[e]; P.Vc[e] = P.Vn[e]; }
+              P.streak++;
+              if (P.streak < c.caution_steps && P.scale > T(1)) P.scale = T(1);
+              P.s *= P.scale;
+              if (P.s > T(c.s_max)) P.s = T(c.s_max);
+              else if (P.s < T(c.s_min)) P.s = T(c.s_min * 0.9);
+              P.step++;
+              if (P.step == c.max_steps) { P.code = 1; finished = true; }
+              else if (LO && P.Yc[NY - 1].re >= T(c.t_switch)) handoff = 1;
+              else { P.stage = 0; P.phase = PH_RK; }
+            }
+          } else {
+            // new random patch and retry (htpytrack.cu:145-153)
+            draw_patch(P.rng, c.patch_range, P.u);
+            switch_patch(P.u, P.Yn, P.Yn);
+            if (++P.attempt < c.newt_attempts) begin_newton(P, PH_NEWTON);
+            else if (P.s <= T(c.s_min)) {
+              if (LO) handoff = 3; else { P.code = 4; finished = true; }
+            } else {
+              P.s *= T(0.5);
+              if (P.s < T(c.s_min)) P.s = T(c.s_min * 0.9);
+              P.streak = 0;
+              P.stage = 0;
+              P.phase = PH_RK;
+            }
+          }
+        } else {
+          final_src = P.YN;
+          if (P.ministep++ == c.max_ministeps) { P.code = 2; finished = true; }
+          else if (P.residual < T(c.sharp_tol)) { P.code = 0; finished = true; }
+          else {
+            draw_patch(P.rng, c.patch_range, P.u);
+            switch_patch(P.u, P.Yn, P.Yn);
+            if (++P.attempt < c.sharp_attempts) begin_newton(P, PH_SHARP);
+            else { P.code = 5; finished = true; }
+          }
+        }
+      }
+    }
+
+    if (LO && handoff) {
+      save_handoff(a, P, handoff);
+      P.phase = PH_FETCH;
+      continue;
+    }
+
+    // ---------------------------------------------------------------- finish
+    if (finished) {
+      cd Yf[NY];
+#pragma unroll 1
+      for (int e = 0; e < NY; ++e) Yf[e] = cd(final_src[e]);
+      finish_path(a, P.id, P.task, P.code, Yf, a.fpm + (size_t)P.task * NP);
+      if (a.work) {
+        a.work[(size_t)P.id * 3 + 0] = P.n_ivp;
+        a.work[(size_t)P.id * 3 + 1] = P.n_newton;
+        a.work[(size_t)P.id * 3 + 2] = P.step;
+      }
+      if (a.counters) {
+        atomicAdd(&a.counters[8], (unsigned long long)P.n_ivp);
+        atomicAdd(&a.counters[9], (unsigned long long)P.n_newton);
+        atomicAdd(&a.counters[10], (unsigned long long)P.step);
+      }
+      P.phase = PH_FETCH;
+    }
+  }
+  // FP64 linear steps of this thread (all of them for MODE_PLAIN and MODE_RESUME)
+  if (a.counters && fp64_solves) atomicAdd(&a.counters[11], fp64_solves);
+}
+
+// Write a finished path: the tracked endpoint (optional), the finite check, the
+// dehomogenized canonical root (frg.cu:44-46, :59-68), its code, and the
+// row-scaled residual of the target system at the root.
+__device__ void finish_path(const TrackArgs& a, int64_t id, int task, int code, cd* Yf, const cd* fpm) {
+  const frg_config& c = a.cfg;
+  if (a.yfinal) {
+#pragma unroll 1
+    for (int e = 0; e < NY; ++e) a.yfinal[(size_t)id * NY + e] = Yf[e];
+  }
+  if (code == 0 && c.inf_tol > 0.0) {
+    double zmax = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < NV; ++e) zmax = fmax(zmax, sqrt(cnorm2(Yf[e])));
+    if (sqrt(cnorm2(Yf[NV])) < c.inf_tol * zmax) code = FRG_CODE_INFINITE;
+  }
+  cd ud[NY];
+#pragma unroll 1
+  for (int e = 0; e < NY; ++e) ud[e] = cd(0.0);
+  ud[NV] = cd(1.0);
+  switch_patch(ud, Yf, Yf);
+  cd root[NV];
+  canonical_cognate(Yf, fpm, root);
+#pragma unroll 1
+  for (int e = 0; e < NV; ++e) a.roots[(size_t)id * NV + e] = root[e];
+  a.codes[id] = code;
+  if (a.counters) atomicAdd(&a.counters[code & 7], 1ull);
+  if (a.resid) {
+    cd Y[NY], q[NP], dq[NP], F[NZ];
+    cd M[NY * LDM];
+#pragma unroll 1
+    for (int e = 0; e < NV; ++e) Y[e] = root[e];
+    Y[NV] = cd(1.0);
+    Y[NV + 1] = cd(1.0);
+#pragma unroll 1
+    for (int e = 0; e < NP; ++e) { q[e] = fpm[e]; dq[e] = cd(0.0); }
+    system_rows<double>(Y, q, dq, M, F);
+    double r = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < NV; ++i) {
+      double mx = 0.0;
+#pragma unroll 1
+      for (int e = 0; e < NZ; ++e) mx = fmax(mx, fmax(fabs(M[i * LDM + e].re), fabs(M[i * LDM + e].im)));
+      r = fmax(r, sqrt(cnorm2(F[i])) / mx);
+    }
+    a.resid[id] = r;
+  }
+}
+
+}  // namespace frg
+
+namespace {
+__global__ void to_float_kernel(const cx<double>* in, cx<float>* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cx<float>(in[i]);
+}
+
+template <int MODE, typename T>
+cudaError_t launch(const frg::TrackArgs& args, int grid, cudaStream_t stream) {
+  frg::track_kernel<MODE, T><<<grid, FRG_TRACK_THREADS, 0, stream>>>(args);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream) {
+  switch (mode) {
+    case frg::MODE_PLAIN: return launch<frg::MODE_PLAIN, double>(args, grid, stream);
+    case frg::MODE_LO: return launch<frg::MODE_LO, float>(args, grid, stream);
+    case frg::MODE_RESUME: return launch<frg::MODE_RESUME, double>(args, grid, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  to_float_kernel<<<(n + 127) / 128, 128, 0, stream>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm) {
+  switch (mode) {
+    case frg::MODE_PLAIN:
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          blocks_per_sm, frg::track_kernel<frg::MODE_PLAIN, double>, FRG_TRACK_THREADS, 0);
+    case frg::MODE_LO:
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          blocks_per_sm, frg::track_kernel<frg::MODE_LO, float>, FRG_TRACK_THREADS, 0);
+    case frg::MODE_RESUME:
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          blocks_per_sm, frg::track_kernel<frg::MODE_RESUME, double>, FRG_TRACK_THREADS, 0);
+    default: return cudaErrorInvalidValue;
+  }
+}

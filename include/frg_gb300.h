@@ -1,0 +1,168 @@
+/*
+ * frg_gb300: GB300-native finite-root-generation path tracker, C ABI.
+ *
+ * The reference (mplecnik/Finite_Root_Generation) has no plugin or FFI layer; its
+ * seam is the set of calls its driver makes each round (frg.cu:351-514):
+ *   InitRandStates + Homotopy kernels          (frg.cu:30-124, launched :361, :374)
+ *   cudaMemcpy of roots and error codes        (frg.cu:389, :398)
+ *   thrust::sort_by_key on Re(root[0])          (frg.cu:432-435)
+ *   SortingDeletingMerging                     (frgsupport.cuh:7, called frg.cu:440)
+ *   LambertW coverage estimate                 (frgsupport.cuh:9, called frg.cu:463-464)
+ *   fptColl / errorCodesAgr persistence        (frg.cu:295-336, :472-480)
+ * Each entry point below names the reference interface it replaces.
+ *
+ * Conventions kept from the reference:
+ *   - complex numbers are interleaved (re, im) doubles (cuDoubleComplex, classes.cuh:24-25);
+ *   - a root is 21 complex values [A,B,C,D,F,G,H, Ac..Hc, U1..U7] = 336 bytes
+ *     (Vect<nV>, htpykinematics.cuh:8), dehomogenized and in canonical cognate form;
+ *   - a task (target parameter set) is 30 complex values
+ *     [P0..P7, Pc0..Pc7, Q1..Q7, Qc1..Qc7] (Vect<nP>, frg.cu:147-178);
+ *   - per-path codes: 0 success, 1 max steps, 2 max ministeps, 3 predictor step
+ *     below s_min, 4 corrector failed at s_min, 5 sharpening failed
+ *     (htpytrack.cu:85,95,100,159,216), 6 duplicate (frgsupport.cu:8), plus
+ *     7 = tracked to an infinite root (only when frg_config.inf_tol > 0);
+ *   - buffers are owned by the caller and may be host or device memory.
+ *
+ * Errors: functions return frg_status; FRG_OK == 0, negative values are argument,
+ * allocation or CUDA errors whose text frg_last_error() returns. One context per
+ * host thread; contexts share no state.
+ */
+#ifndef FRG_GB300_H
+#define FRG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FRG_NV 21 /* unknowns per root (htpykinematics.cuh:8) */
+#define FRG_NP 30 /* parameters per task (htpykinematics.cuh:9) */
+#define FRG_NY 23 /* tracked state: 21 unknowns, homogenizer, t */
+
+typedef enum {
+  FRG_OK = 0,
+  FRG_ERR_ARG = -1,
+  FRG_ERR_ALLOC = -2,
+  FRG_ERR_CUDA = -3,
+  FRG_ERR_IO = -4,
+  FRG_ERR_TIMEOUT = 1
+} frg_status;
+
+enum { FRG_CODE_OK = 0, FRG_CODE_MAX_STEPS = 1, FRG_CODE_MAX_MINISTEPS = 2, FRG_CODE_RK_SMIN = 3,
+       FRG_CODE_NEWTON_SMIN = 4, FRG_CODE_SHARPEN = 5, FRG_CODE_DUPLICATE = 6, FRG_CODE_INFINITE = 7 };
+
+enum { FRG_PREC_FP64 = 0, FRG_PREC_MIXED = 1 };
+enum { FRG_START_UNIFORM = 0, FRG_START_NORMAL = 1 };
+enum { FRG_GAMMA_FIXED = 0, FRG_GAMMA_RANDOM = 1 };
+
+/* Run configuration. frg_config_default() fills the reference's compile-time
+ * constants: tracker settings htpytrack.cu:9-31, start range frgkinematics.cu:7-8,
+ * gamma frg.cu:41, duplicate tolerance frgsupport.cu:7. */
+typedef struct frg_config {
+  double s_init, s_max, s_min, rk_tol;
+  int caution_steps;
+  int newt_its;
+  double newt_tol;
+  int newt_residual; /* 0: |H|, 1: |dY| */
+  int newt_attempts;
+  int sharp_its;
+  double sharp_tol;
+  int sharp_residual;
+  int sharp_attempts;
+  double sharp_trigger, nudge_trigger;
+  int max_steps, max_ministeps;
+  double patch_range;   /* patches uniform in (-r, r)^2 */
+  int start_dist;       /* FRG_START_UNIFORM (reference) or FRG_START_NORMAL */
+  double start_range;   /* uniform start range r: values in (-r, r)^2 */
+  int gamma_mode;       /* FRG_GAMMA_FIXED uses gamma_re/im; FRG_GAMMA_RANDOM draws e^{i phi} per task */
+  double gamma_re, gamma_im;
+  double dup_tol;       /* absolute per-component duplicate tolerance */
+  int precision;        /* FRG_PREC_FP64 (reference arithmetic) or FRG_PREC_MIXED */
+  double t_switch;      /* mixed: FP64 tracking once t exceeds this */
+  double cond_switch;   /* mixed: FP64 corrector when the LU pivot ratio exceeds this */
+  double inf_tol;       /* > 0: |Z0| / |Z| below this at t = 1 marks code 7 */
+  int threads_per_block; /* 0 = tuned default */
+  int blocks_per_sm;     /* 0 = tuned default */
+  double newt_tol_lo;    /* mixed: corrector tolerance of the FP32 stage */
+} frg_config;
+
+/* Per-call counters (all paths of the call). */
+typedef struct frg_stats {
+  int64_t paths;
+  int64_t codes[8];        /* number of paths ending with each code */
+  int64_t ivp_solves;      /* 23x23 tangent solves (predictor stages + initial tangent) */
+  int64_t newton_iters;    /* 22x22 corrector / sharpening solves */
+  int64_t fp64_solves;     /* of the above, solves done in FP64 (mixed precision) */
+  int64_t steps;           /* accepted steps */
+  double track_ms;         /* device time of the tracking kernel(s) */
+  double total_ms;         /* wall time of the call, copies included */
+  int64_t handoffs;        /* mixed precision: paths continued in FP64 */
+} frg_stats;
+
+typedef struct frg_ctx frg_ctx;
+
+/* Fill cfg with the reference's defaults. */
+frg_status frg_config_default(frg_config* cfg);
+
+/* Create a context on CUDA device `device` (replaces the reference's implicit
+ * device 0 and its cudaMalloc block, frg.cu:139, :201-236). */
+frg_status frg_create(frg_ctx** ctx, const frg_config* cfg, int device);
+void frg_destroy(frg_ctx* ctx);
+const char* frg_last_error(const frg_ctx* ctx);
+frg_status frg_set_config(frg_ctx* ctx, const frg_config* cfg);
+
+/* Track paths (replaces InitRandStates + Homotopy + the two copies back,
+ * frg.cu:30-124, :361-404). Path i of task k uses random stream
+ * (sum of paths of earlier tasks) + i of `seed`; the reference's per-thread curand
+ * subsequence i (frg.cu:32).
+ *   fpm            ntasks x 30 complex target parameters
+ *   paths_per_task ntasks counts; total N = sum
+ *   roots          out, N x 21 complex (canonical cognate, dehomogenized, frg.cu:59-68)
+ *   codes          out, N int32
+ *   yfinal         optional out, N x 23 complex tracked endpoints before dehomogenizing
+ *   resid          optional out, N doubles: max |F_r| / max_c |dF_r/dZ_c| at the root
+ *   stats          optional out
+ * Pointers may be host or device memory (probed). Synchronous. */
+frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                     uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
+                     frg_stats* stats);
+
+/* Same, enqueued on `stream` (a cudaStream_t); device pointers only, returns
+ * before the work completes. */
+frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                           uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
+                           void* stream);
+
+/* ---- root collection (replaces SortingDeletingMerging, frgsupport.cu:10-215, and
+ *      the thrust ordering of frg.cu:432-435) ---- */
+typedef struct frg_coll frg_coll;
+
+frg_status frg_coll_create(frg_coll** coll, double dup_tol);
+void frg_coll_destroy(frg_coll* coll);
+int64_t frg_coll_size(const frg_coll* coll);
+/* Copy the sorted collection (size x 21 complex) to host memory `out`. */
+frg_status frg_coll_get(const frg_coll* coll, double* out, int64_t capacity);
+/* Merge one round of roots into the collection: successes (code 0) that duplicate a
+ * collected root, or an earlier success of the round, within dup_tol in every real
+ * component become code 6 in place; the others are added. Host memory. */
+frg_status frg_coll_merge(frg_coll* coll, const double* roots, int32_t* codes, int64_t n);
+/* Persistence in the reference's byte formats: fptColl = raw roots, 336 bytes each,
+ * sorted; errorCodesAgr = int32 per trial, appended (frg.cu:295-336, :472-480). */
+frg_status frg_coll_save(const frg_coll* coll, const char* fpt_coll_path);
+frg_status frg_coll_load(frg_coll* coll, const char* fpt_coll_path);
+frg_status frg_codes_append(const char* error_codes_path, const int32_t* codes, int64_t n);
+
+/* ---- statistics (frgsupport.cu:220-272, frg.cu:463-464) ---- */
+/* Principal branch of the Lambert W function. */
+double frg_lambertw0(double z);
+/* Estimated fraction of all roots collected, s W(-e^{-1/s}/s) + 1 with
+ * s = successes / (successes + duplicates). */
+double frg_estimate_collected(int64_t successes, int64_t duplicates);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FRG_GB300_H */

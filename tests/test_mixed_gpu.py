@@ -1,0 +1,62 @@
+"""Mixed precision (FP32 stage, FP64 endgame/sharpening) against plain FP64 on the
+same tasks and seeds: recall of distinct finite roots, residuals, FP64 share."""
+import numpy as np
+import pytest
+
+import finite_root_generation_gb300 as frg
+from finite_root_generation_gb300 import build as frg_build
+from finite_root_generation_gb300.metrics import distinct_roots, recall
+from finite_root_generation_gb300.tasks import REFERENCE_TARGET, precision_point_task
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(precision, **kw):
+    return frg.default_config(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=1e-8,
+                              precision=precision, **kw)
+
+
+@pytest.fixture(scope="module")
+def runs():
+    frg_build.build()
+    task = precision_point_task(1, "disk")
+    n = 4096
+    out = {}
+    for name, prec in (("fp64", frg.PREC_FP64), ("mixed", frg.PREC_MIXED)):
+        with frg.Tracker(_cfg(prec)) as t:
+            out[name] = t.track(task, [n], 4242, want_resid=True)
+    return out
+
+
+def test_mixed_recall_vs_fp64(runs):
+    a = distinct_roots(runs["fp64"].roots, runs["fp64"].codes, runs["fp64"].resid)
+    b = distinct_roots(runs["mixed"].roots, runs["mixed"].codes, runs["mixed"].resid)
+    assert len(a) > 0.9 * 4096
+    r = recall(a, b)
+    assert r >= 0.99, r
+    assert len(b) >= 0.99 * len(a)
+
+
+def test_mixed_residuals(runs):
+    res = runs["mixed"]
+    ok = res.codes == 0
+    assert ok.mean() > 0.9
+    assert np.all(res.resid[ok] <= 1e-10)
+
+
+def test_mixed_uses_fp32_for_most_solves(runs):
+    s = runs["mixed"].stats
+    total = s["ivp_solves"] + s["newton_iters"]
+    assert 0 < s["handoffs"] <= s["paths"]
+    assert s["fp64_solves"] < 0.5 * total
+    assert runs["fp64"].stats["fp64_solves"] == runs["fp64"].stats["ivp_solves"] + runs["fp64"].stats["newton_iters"]
+
+
+def test_mixed_reference_target():
+    """Mixed precision on the reference's own target and gamma finds the reference's roots."""
+    with frg.Tracker(frg.default_config(precision=frg.PREC_MIXED)) as t:
+        m = t.track(REFERENCE_TARGET, [512], 1234, want_resid=True)
+    with frg.Tracker(frg.default_config()) as t:
+        p = t.track(REFERENCE_TARGET, [512], 1234, want_resid=True)
+    r = recall(distinct_roots(p.roots, p.codes, p.resid), distinct_roots(m.roots, m.codes, m.resid))
+    assert r >= 0.98, r
