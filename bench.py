@@ -1,9 +1,9 @@
 """Benchmark: distinct finite roots per second on one GB300.
 
-Workload (one "step" = one round of the tracker): 65,536 paths on one precision-
-point task (seed 1: 8 points uniform in the unit disk, unit crank rotations), start
-mechanisms from complex normal link/pivot values, a random unit-modulus gamma, FP64
-tracking with sharpening to 1e-12 at t = 1, canonical cognates, finite-root check
+Workload (one "step" = one round of the tracker): 65,536 paths on one generic
+precision-point task (seed 1: P_k and Pc_k uniform in the unit disk, crank rotations
+on the unit circle), start mechanisms from complex normal link/pivot values, a random
+unit-modulus gamma, sharpening to 1e-12 at t = 1 in FP64, canonical cognates, finite-root check
 (|Z0|/|Z| >= 1e-8), per-root residual, and duplicate removal in a root collection.
 A root counts when its path succeeded, it is finite, its row-scaled residual is
 <= 1e-10, and it is not a duplicate. Synthetic inputs: the reference ships no
@@ -11,7 +11,9 @@ benchmark data; tasks and starts are seeded.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--paths P] [--impl ours|reference]
 
-value    distinct finite roots / second of device tracking time (inputs resident in HBM)
+value    distinct finite roots / second of device tracking time (inputs resident in HBM) of the
+         chosen configuration: mixed precision (FP32 team stage, FP64 endgame and sharpening);
+         plain FP64 on the same seeds gives `plain_fp64`, the speed-up and the recall
 e2e      the same through the public C ABI with host buffers: per step the task upload,
          tracking, the copy of roots/codes/residuals back and the host duplicate merge
 --impl reference  times the reference algorithm's CPU implementation (the C
@@ -115,25 +117,27 @@ class ClockSampler:
 
 # ------------------------------------------------------------------------ FP64 peak
 FMA_PEAK_SRC = r"""
-extern "C" __global__ void fma_peak_f64(double* out, int iters, double a, double b) {
-  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-3, x2 = x0 + 2e-3, x3 = x0 + 3e-3;
-  double x4 = x0 + 4e-3, x5 = x0 + 5e-3, x6 = x0 + 6e-3, x7 = x0 + 7e-3;
+template <typename T>
+__global__ void fma_peak(T* out, int iters, T a, T b) {
+  T x0 = threadIdx.x * T(1e-9), x1 = x0 + T(1e-3), x2 = x0 + T(2e-3), x3 = x0 + T(3e-3);
+  T x4 = x0 + T(4e-3), x5 = x0 + T(5e-3), x6 = x0 + T(6e-3), x7 = x0 + T(7e-3);
   for (int i = 0; i < iters; ++i) {
     x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
     x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
   }
-  if (x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7 == 123.0) out[0] = x0;
+  if (x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7 == T(123)) out[0] = x0;
 }
 """
 
 
-def measure_fp64_peak():
-    """Dense FP64 FMA throughput of this GPU (TFLOP/s), measured with a chain-free
-    DFMA kernel. MEASURED_PEAKS.json records only HBM and bf16 tensor peaks."""
+def measure_fma_peaks():
+    """Dense FP64 and FP32 FMA throughput of this GPU (TFLOP/s), measured with
+    8 independent FMA chains per thread. MEASURED_PEAKS.json records only HBM and
+    bf16 tensor peaks, so the FMA-pipe denominators are measured here."""
     from finite_root_generation_gb300 import build as frg_build
 
     import ctypes
-    so = os.path.join(frg_build.BUILD, "fma_peak.so")
+    so = os.path.join(frg_build.BUILD, "fma_peak2.so")
     os.makedirs(frg_build.BUILD, exist_ok=True)
     src = os.path.join(frg_build.BUILD, "fma_peak.cu")
     if not os.path.exists(so):
@@ -141,16 +145,20 @@ def measure_fp64_peak():
             f.write(FMA_PEAK_SRC)
             f.write(r"""
 #include <cuda_runtime.h>
-extern "C" float run_fma_peak(int blocks, int threads, int iters) {
-  double* out; cudaMalloc(&out, 8);
+template <typename T>
+static float run(int blocks, int threads, int iters) {
+  T* out; cudaMalloc(&out, 8);
   cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
-  fma_peak_f64<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  fma_peak<T><<<blocks, threads>>>(out, iters, T(0.999999), T(1e-7));
   cudaEventRecord(e0);
-  fma_peak_f64<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  fma_peak<T><<<blocks, threads>>>(out, iters, T(0.999999), T(1e-7));
   cudaEventRecord(e1); cudaEventSynchronize(e1);
   float ms; cudaEventElapsedTime(&ms, e0, e1);
   cudaFree(out); cudaEventDestroy(e0); cudaEventDestroy(e1);
   return ms;
+}
+extern "C" float run_fma_peak(int fp64, int blocks, int threads, int iters) {
+  return fp64 ? run<double>(blocks, threads, iters) : run<float>(blocks, threads, iters);
 }
 """)
         subprocess.run([frg_build.nvcc(), *frg_build.ARCH, "-O3", "-Xcompiler", "-fPIC", "-shared", src, "-o", so],
@@ -159,49 +167,70 @@ extern "C" float run_fma_peak(int blocks, int threads, int iters) {
     lib.run_fma_peak.restype = ctypes.c_float
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, threads, iters = sms * 8, 256, 4096
-    ms = lib.run_fma_peak(blocks, threads, iters)
-    flops = 2.0 * 8 * iters * blocks * threads
-    return flops / (ms * 1e-3) / 1e12
+    out = {}
+    for name, fp64, iters in (("fp64", 1, 4096), ("fp32", 0, 65536)):
+        blocks, threads = sms * 8, 256
+        ms = lib.run_fma_peak(fp64, blocks, threads, iters)
+        out[name] = 2.0 * 8 * iters * blocks * threads / (ms * 1e-3) / 1e12
+    return out
 
 
 # ------------------------------------------------------------------ algorithmic work
-def algorithmic_flops(ivp_solves, newton_iters):
-    """Algorithmic FLOPs of the linear-system steps, counting complex mul = 6, complex
-    add = 2, real x complex = 2, complex fused multiply-add = 8 (the same convention
-    for every variant; zeros of the Jacobian are not counted):
-      system  = 7 groups of the generated code (FRG_GEN_* in frg_system_gen.cuh) + 4 reciprocals
-      params  = q(t), dq/dt for 30 parameters
-      scale   = 22 x 23 real x complex
-      LU(ne)  = sum_i (ne-i-1)[(23-i-1) cfma + l + rhs] + back substitution
-    """
-    gen = open(os.path.join(ROOT, "finite_root_generation_gb300", "csrc", "frg_system_gen.cuh")).read()
+def _gen_counts():
     import re
-    cm = int(re.search(r"#define FRG_GEN_CMUL (\d+)", gen).group(1))
-    ca = int(re.search(r"#define FRG_GEN_CADD (\d+)", gen).group(1))
-    sm = int(re.search(r"#define FRG_GEN_SMUL (\d+)", gen).group(1))
-    w_sys = 7 * (6 * cm + 2 * ca + 2 * sm + 12) + 4 * 12
-    w_par = 30 * 24
-    w_scale = 22 * 23 * 2
+    gen = open(os.path.join(ROOT, "finite_root_generation_gb300", "csrc", "frg_system_gen.cuh")).read()
+    return tuple(int(re.search(rf"#define FRG_GEN_{k} (\d+)", gen).group(1)) for k in ("CMUL", "CADD", "SMUL"))
 
-    def lu(ne, n=23):
-        f = 0
-        for i in range(ne):
-            f += (ne - i - 1) * ((n - i - 1) * 8 + 6 + 8)
-        for i in range(n if ne == n else n - 1):
-            f += (n - i - 1) * 8 + 6 + 2
-        return f
-    w_ivp = w_par + w_sys + w_scale + lu(23) + 23 * 8
-    w_newton = w_par + w_sys + w_scale + lu(22) + 23 * 4
-    return ivp_solves * w_ivp + newton_iters * w_newton, {"ivp": w_ivp, "newton": w_newton}
+
+def flops_per_solve():
+    """Algorithmic FLOPs of one linear-system step of the team kernels, counting
+    complex mul = 6, complex add = 2, real x complex = 2, complex FMA = 8, complex
+    reciprocal = 12; zeros are not counted and work repeated across lanes counts once:
+      params   q(t), dq/dt of 30 parameters                          30 x 24
+      system   7 groups of generated code (FRG_GEN_* counts) + 11 reciprocals
+      scale    21 group rows x 18 entries + the u row (23)           x 2
+      group    7 x [1 reciprocal + 2 rows x (1 cmul + 17 cfma)]
+      fold     7 x 2 patch rows x (1 + 17) cmul + 7 x 2 x 17 complex adds
+      LU16     sum_k (15-k) x (cmul + (16-k) cfma) + 16 reciprocals
+      backsub  sum_k (6 + 8 k); U recovery 7 x (16 cfma + 1 cmul)
+      norm     23 x (cmul + |.|^2)
+    A Newton iteration has the same structure (the t-selector replaces the velocity
+    patch), so both kinds of step count the same."""
+    cm, ca, sm = _gen_counts()
+    f = 30 * 24
+    f += 7 * (6 * cm + 2 * ca + 2 * sm) + 11 * 12
+    f += (21 * 18 + 23) * 2
+    f += 7 * (12 + 2 * (6 + 17 * 8))
+    f += 7 * 2 * 18 * 6 + 7 * 2 * 17 * 2
+    f += sum((15 - k) * (6 + 8 * (16 - k)) for k in range(16)) + 16 * 12
+    f += sum(6 + 8 * k for k in range(16)) + 7 * (16 * 8 + 6)
+    f += 23 * (6 + 4)
+    return f
 
 
 # ---------------------------------------------------------------------- our impl
+def _track_steps(frg, torch, tracker, task, n, seeds, bufs, flush):
+    """Run one step per seed into device buffers; returns per-step stats and the
+    distinct finite roots of each step (computed on the host after the timed kernels)."""
+    d_fpm, d_roots, d_codes, d_resid = bufs
+    stats, sets = [], []
+    for sd in seeds:
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = tracker.track_into(d_fpm, [n], sd, d_roots, d_codes, resid=d_resid)
+        stats.append(st)
+        roots = d_roots.cpu().numpy().view(np.complex128)
+        from finite_root_generation_gb300.metrics import distinct_roots
+        sets.append(distinct_roots(roots, d_codes.cpu().numpy(), d_resid.cpu().numpy(), RESID_MAX))
+    return stats, sets
+
+
 def run_ours(args, rank, world):
     import torch
 
     import finite_root_generation_gb300 as frg
     from finite_root_generation_gb300 import build as frg_build
+    from finite_root_generation_gb300.metrics import distinct_roots, recall
     from finite_root_generation_gb300.tasks import precision_point_task
 
     frg_build.build()
@@ -209,38 +238,34 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     task = precision_point_task(TASK_SEED, "disk")
     n = args.paths
-    tracker = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
-    d_fpm = torch.from_numpy(task.view(np.float64).copy()).cuda()
-    d_roots = torch.empty((n, 42), dtype=torch.float64, device="cuda")
-    d_codes = torch.empty(n, dtype=torch.int32, device="cuda")
-    d_resid = torch.empty(n, dtype=torch.float64, device="cuda")
+    chosen = frg.Tracker(workload_config(frg, frg.PREC_MIXED), device=dev)
+    plain = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
+    bufs = (torch.from_numpy(task.view(np.float64).copy()).cuda(),
+            torch.empty((n, 42), dtype=torch.float64, device="cuda"),
+            torch.empty(n, dtype=torch.int32, device="cuda"),
+            torch.empty(n, dtype=torch.float64, device="cuda"))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def seed_of(step):
         return 1000003 * (rank + 1) + step
 
     for w in range(args.warmup):
-        tracker.track_into(d_fpm, [n], seed_of(-1 - w), d_roots, d_codes, resid=d_resid)
+        chosen.track_into(bufs[0], [n], seed_of(-1 - w), bufs[1], bufs[2], resid=bufs[3])
+    plain.track_into(bufs[0], [min(n, 8192)], seed_of(-1), bufs[1], bufs[2], resid=bufs[3])
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
 
-    # ---- device-resident timing (value) ----
-    track_ms, distinct, ivp, newt, launches = 0.0, 0, 0, 0, 0
+    # ---- chosen configuration, device-resident (value) ----
+    seeds = [seed_of(k) for k in range(args.steps)]
     with ClockSampler(dev) as clk:
-        for step in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            st = tracker.track_into(d_fpm, [n], seed_of(step), d_roots, d_codes, resid=d_resid)
-            launches += 1
-            track_ms += st["track_ms"]
-            ivp += st["ivp_solves"]
-            newt += st["newton_iters"]
-            roots = d_roots.cpu().numpy().view(np.complex128)
-            d, _ = count_distinct(frg, roots, d_codes.cpu().numpy(), d_resid.cpu().numpy())
-            distinct += d
+        c_stats, c_sets = _track_steps(frg, torch, chosen, task, n, seeds, bufs, flush)
     torch.cuda.synchronize()
     clocks = clk.summary()
+    # ---- plain FP64 on the same seeds (ratio and recall) ----
+    p_seeds = seeds[: max(1, args.plain_steps)]
+    p_stats, p_sets = _track_steps(frg, torch, plain, task, n, p_seeds, bufs, flush)
+    rec = [recall(p_sets[i], c_sets[i]) for i in range(len(p_seeds))]
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
     h_roots = np.zeros((n, 21), np.complex128)
@@ -251,48 +276,84 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for step in range(args.steps):
-        tracker.track_into(task, [n], seed_of(step), h_roots, h_codes, resid=h_resid)
-        d, _ = count_distinct(frg, h_roots, h_codes, h_resid)
-        e2e_distinct += d
+    for sd in seeds:
+        chosen.track_into(task, [n], sd, h_roots, h_codes, resid=h_resid)
+        e2e_distinct += len(distinct_roots(h_roots, h_codes, h_resid, RESID_MAX))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
-    t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, ivp, newt], dtype=torch.float64)
+    track_ms = sum(st["track_ms"] for st in c_stats)
+    distinct = sum(len(d) for d in c_sets)
+    p_ms = sum(st["track_ms"] for st in p_stats)
+    p_distinct = sum(len(d) for d in p_sets)
+    t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct], dtype=torch.float64)
     if world > 1:
-        tmax = t.clone().cuda()
-        tsum = t.clone().cuda()
+        tmax, tsum = t.clone().cuda(), t.clone().cuda()
         torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        track_ms, e2e_s = float(tmax[0]), float(tmax[1])
-        distinct, e2e_distinct, ivp, newt = (float(x) for x in tsum[2:6])
-    tracker.close()
+        track_ms, e2e_s, p_ms = float(tmax[0]), float(tmax[1]), float(tmax[4])
+        distinct, e2e_distinct, p_distinct = float(tsum[2]), float(tsum[3]), float(tsum[5])
+    chosen.close()
+    plain.close()
     if rank != 0:
         return None
 
     value = distinct / (track_ms * 1e-3)
+    value_plain = p_distinct / (p_ms * 1e-3)
     e2e = e2e_distinct / e2e_s
-    flops, per = algorithmic_flops(ivp / world, newt / world)
-    achieved = flops / (track_ms / args.steps * 1e-3) / args.steps / 1e12  # per launch / launch time
-    peak = measure_fp64_peak()
-    h2d = 16 * 30 + 16 + 16  # task, gamma, task offsets
+    # roofline of each kernel: algorithmic FLOPs per launch / launch time
+    peaks = measure_fma_peaks()
+    fps = flops_per_solve()
+    k = args.steps
+    solves = sum(st["ivp_solves"] + st["newton_iters"] for st in c_stats) / k
+    fp64_solves = sum(st["fp64_solves"] for st in c_stats) / k
+    fp32_solves = solves - fp64_solves
+    ms32 = sum(st["stage_ms"][0] for st in c_stats) / k
+    ms64 = sum(st["stage_ms"][1] for st in c_stats) / k
+    kernels = {
+        "team_kernel<MODE_LO, float> (FP32 stage)": {
+            "bound": "fp32", "achieved": fp32_solves * fps / (ms32 * 1e-3) / 1e12, "peak": peaks["fp32"],
+            "ms_per_launch": ms32, "solves_per_launch": fp32_solves},
+        "team_kernel<MODE_RESUME, double> (FP64 stage)": {
+            "bound": "fp64", "achieved": fp64_solves * fps / (ms64 * 1e-3) / 1e12, "peak": peaks["fp64"],
+            "ms_per_launch": ms64, "solves_per_launch": fp64_solves},
+    }
+    for v in kernels.values():
+        v["frac"] = v["achieved"] / v["peak"]
+    dom_name = max(kernels, key=lambda kk: kernels[kk]["ms_per_launch"])
+    dom = kernels[dom_name]
+    p_solves = sum(st["ivp_solves"] + st["newton_iters"] for st in p_stats) / len(p_stats)
+    p_ms_launch = p_ms / len(p_stats)
+    plain_roof = p_solves * fps / (p_ms_launch * 1e-3) / 1e12
+    h2d = 16 * 30 + 16 + 16
     d2h = n * (16 * 21 + 4 + 8)
     line = {
-        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(track_ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tasks and starts)",
-        "config": {"workload": f"Stephenson II FRG round: {n} paths, 1 precision-point task (seed {TASK_SEED}), "
-                               "complex-normal starts, random gamma, FP64 + sharpening + dedup",
-                   "paths_per_step": n, "precision": "plain FP64", "l2": "flushed (256 MB write) between steps",
-                   "parallelism": f"replicas x{world} (independent paths)"},
-        "distinct_roots_per_step": distinct / args.steps / world,
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": k,
+        "warmup": args.warmup, "ms_per_step": round(track_ms / k, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded task and start mechanisms)",
+        "config": {"workload": f"Stephenson II FRG round: {n} paths on 1 generic complex precision-point task "
+                               f"(seed {TASK_SEED}), complex-normal start mechanisms, random unit gamma; "
+                               "sharpening to 1e-12 in FP64, canonical cognates, finite + residual <= 1e-10 "
+                               "checks, duplicate removal",
+                   "paths_per_step": n, "chosen": "mixed precision (FP32 team stage, FP64 endgame), team kernels",
+                   "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{world}"},
+        "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": len(p_seeds),
+                       "ms_per_step": round(p_ms_launch, 3),
+                       "roofline_frac_fp64": round(plain_roof / peaks["fp64"], 4)},
+        "speedup_vs_plain_fp64": round(value / value_plain, 3),
+        "recall_vs_plain_fp64": round(min(rec), 5),
+        "distinct_roots_per_step": distinct / k / world,
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "fp64", "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
-                     "peak_source": "FP64 FMA peak measured live by bench.py (MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_ivp_solve": per["ivp"], "flops_per_newton_iter": per["newton"],
-                     "solves_per_launch": (ivp + newt) / world / args.steps},
-        "gpu_launches": launches,
+        "roofline": {"kernel": dom_name, "bound": dom["bound"], "achieved": round(dom["achieved"], 4),
+                     "peak": round(dom["peak"], 4), "unit": "TFLOP/s", "frac": round(dom["frac"], 4),
+                     "traffic": None,
+                     "peak_source": "FMA peaks measured live by bench.py (MEASURED_PEAKS.json has no FP32/FP64 "
+                                    "vector figure)",
+                     "flops_per_solve": fps,
+                     "kernels": {kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
+                                 for kk, v in kernels.items()}},
+        "gpu_launches": 3 * k,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -365,6 +426,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--paths", type=int, default=65536)
     ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -27,6 +27,7 @@ CODE_NAMES = {0: "success", 1: "max steps", 2: "max ministeps", 3: "predictor st
 PREC_FP64, PREC_MIXED = 0, 1
 START_UNIFORM, START_NORMAL = 0, 1
 GAMMA_FIXED, GAMMA_RANDOM = 0, 1
+KERNEL_TEAM, KERNEL_THREAD = 0, 1
 
 _D = ctypes.POINTER(ctypes.c_double)
 _I32 = ctypes.POINTER(ctypes.c_int32)
@@ -56,7 +57,7 @@ class FrgConfig(ctypes.Structure):
         ("precision", ctypes.c_int), ("t_switch", ctypes.c_double), ("cond_switch", ctypes.c_double),
         ("inf_tol", ctypes.c_double),
         ("threads_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-        ("newt_tol_lo", ctypes.c_double),
+        ("newt_tol_lo", ctypes.c_double), ("kernel_variant", ctypes.c_int),
     ]
 
 
@@ -67,12 +68,14 @@ class FrgStats(ctypes.Structure):
         ("paths", ctypes.c_int64), ("codes", ctypes.c_int64 * 8), ("ivp_solves", ctypes.c_int64),
         ("newton_iters", ctypes.c_int64), ("fp64_solves", ctypes.c_int64), ("steps", ctypes.c_int64),
         ("track_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("handoffs", ctypes.c_int64),
+        ("stage_ms", ctypes.c_double * 2), ("handoff_reason", ctypes.c_int64 * 6),
     ]
 
     def as_dict(self) -> dict:
         return {"paths": self.paths, "codes": list(self.codes), "ivp_solves": self.ivp_solves,
                 "newton_iters": self.newton_iters, "fp64_solves": self.fp64_solves, "steps": self.steps,
-                "track_ms": self.track_ms, "total_ms": self.total_ms, "handoffs": self.handoffs}
+                "track_ms": self.track_ms, "total_ms": self.total_ms, "handoffs": self.handoffs,
+                "stage_ms": list(self.stage_ms), "handoff_reason": list(self.handoff_reason)}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.

@@ -51,9 +51,10 @@ struct frg_ctx {
   int device = 0;
   frg_config cfg;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evmid = nullptr;
   int sm_count = 0;
-  int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each kernel mode
+  int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each thread-per-path kernel mode
+  int team_blocks_per_sm[3] = {0, 0, 0};
   std::string err;
   DevBuf fpm, gamma, fpm_lo, gamma_lo, task_start, queue, counters, roots, codes, yfinal, resid;
   DevBuf handoff, handoff_list;
@@ -114,6 +115,8 @@ static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
     return fail(ctx, FRG_ERR_ARG, "unknown gamma_mode");
   if (c->precision != FRG_PREC_FP64 && c->precision != FRG_PREC_MIXED)
     return fail(ctx, FRG_ERR_ARG, "unknown precision");
+  if (c->kernel_variant != FRG_KERNEL_TEAM && c->kernel_variant != FRG_KERNEL_THREAD)
+    return fail(ctx, FRG_ERR_ARG, "unknown kernel_variant");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   return FRG_OK;
@@ -135,9 +138,12 @@ extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int devic
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->evmid);
   for (int m = 0; m < 3 && e == cudaSuccess; ++m) {
     e = frg_track_occupancy(m, &ctx->blocks_per_sm[m]);
     if (ctx->blocks_per_sm[m] < 1) ctx->blocks_per_sm[m] = 1;
+    if (e == cudaSuccess) e = frg_team_occupancy(m, &ctx->team_blocks_per_sm[m]);
+    if (ctx->team_blocks_per_sm[m] < 1) ctx->team_blocks_per_sm[m] = 1;
   }
   if (e != cudaSuccess) {
     frg_destroy(ctx);
@@ -157,6 +163,7 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
     b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->evmid) cudaEventDestroy(ctx->evmid);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -201,14 +208,14 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   FRG_CUDA(ctx, ctx->fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
   FRG_CUDA(ctx, ctx->task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
   FRG_CUDA(ctx, ctx->queue.ensure(sizeof(unsigned long long) * 4));
-  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 16));
+  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 24));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma.p, g.data(), sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_lo.p, g_lo.data(), sizeof(cx<float>) * ntasks, cudaMemcpyHostToDevice,
                                 st));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->task_start.p, starts.data(), sizeof(int64_t) * (ntasks + 1),
                                 cudaMemcpyHostToDevice, st));
   FRG_CUDA(ctx, cudaMemsetAsync(ctx->queue.p, 0, sizeof(unsigned long long) * 4, st));
-  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 16, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 24, st));
   FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)ctx->fpm_lo.p, FRG_NP * ntasks, st));
 
   frg::TrackArgs a;
@@ -230,15 +237,23 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   a.resid = d_resid;
   a.work = nullptr;
   a.counters = (unsigned long long*)ctx->counters.p;
+  const bool team = ctx->cfg.kernel_variant == FRG_KERNEL_TEAM;
+  // persistent grids: SMs x resident blocks, capped by the work (one path per thread
+  // for the thread kernels, one per 8 lanes for the team kernels)
   auto grid_for = [&](int mode, int64_t n) {
-    int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm : ctx->blocks_per_sm[mode];
+    int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm
+                                         : (team ? ctx->team_blocks_per_sm[mode] : ctx->blocks_per_sm[mode]);
     int64_t grid = (int64_t)ctx->sm_count * bps;
-    int64_t need = (n + FRG_TRACK_THREADS - 1) / FRG_TRACK_THREADS;
+    int64_t per_block = team ? FRG_TEAM_THREADS / 8 : FRG_TRACK_THREADS;
+    int64_t need = (n + per_block - 1) / per_block;
     if (grid > need) grid = need;
     return (int)(grid < 1 ? 1 : grid);
   };
+  auto launch = [&](int mode, int grid) {
+    return team ? frg_launch_team(mode, a, grid, st) : frg_launch_track(mode, a, grid, st);
+  };
   if (!mixed) {
-    cudaError_t e = frg_launch_track(0, a, grid_for(0, N), st);
+    cudaError_t e = launch(0, grid_for(0, N));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64)");
     return FRG_OK;
   }
@@ -248,10 +263,11 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   a.handoff_list = (int64_t*)ctx->handoff_list.p;
   a.handoff_count = q + 2;
   a.queue = q;
-  cudaError_t e = frg_launch_track(1, a, grid_for(1, N), st);
+  cudaError_t e = launch(1, grid_for(1, N));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
+  FRG_CUDA(ctx, cudaEventRecord(ctx->evmid, st));
   a.queue = q + 1;
-  e = frg_launch_track(2, a, grid_for(2, N), st);
+  e = launch(2, grid_for(2, N));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
   return FRG_OK;
 }
@@ -326,7 +342,7 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
   FRG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   for (Out& o : outs)
     if (o.user && o.host) FRG_CUDA(ctx, cudaMemcpyAsync(o.user, o.dev, o.bytes, cudaMemcpyDeviceToHost, st));
-  unsigned long long cnt[16], qv[4];
+  unsigned long long cnt[24], qv[4];
   FRG_CUDA(ctx, cudaMemcpyAsync(cnt, ctx->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
   FRG_CUDA(ctx, cudaMemcpyAsync(qv, ctx->queue.p, sizeof(qv), cudaMemcpyDeviceToHost, st));
   FRG_CUDA(ctx, cudaStreamSynchronize(st));
@@ -336,10 +352,21 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
     stats->newton_iters = (int64_t)cnt[9];
     stats->steps = (int64_t)cnt[10];
     stats->fp64_solves = (int64_t)cnt[11];
-    stats->handoffs = ctx->cfg.precision == FRG_PREC_MIXED ? (int64_t)qv[2] : 0;
+    stats->handoffs = (int64_t)cnt[12];
+    for (int r = 0; r < 6; ++r) stats->handoff_reason[r] = (int64_t)cnt[16 + r];
+    (void)qv;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->track_ms = ms;
+    if (ctx->cfg.precision == FRG_PREC_MIXED) {
+      float m0 = 0.f, m1 = 0.f;
+      cudaEventElapsedTime(&m0, ctx->ev0, ctx->evmid);
+      cudaEventElapsedTime(&m1, ctx->evmid, ctx->ev1);
+      stats->stage_ms[0] = m0;
+      stats->stage_ms[1] = m1;
+    } else {
+      stats->stage_ms[1] = ms;
+    }
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return FRG_OK;

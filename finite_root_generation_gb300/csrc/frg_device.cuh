@@ -21,6 +21,24 @@ constexpr int LDM = 24; // leading dimension of the 23x23 system (+ right-hand s
 
 typedef cx<double> cd;
 
+// Dormand-Prince 6(5) tableau (rungekutta.cu:261-341): stage weights, error
+// weights (LTE, :318-324) and 6th-order solution weights (:334-341).
+static __constant__ double c_dpA[8][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {1. / 10., 0, 0, 0, 0, 0, 0},
+    {-2. / 81., 20. / 81., 0, 0, 0, 0, 0},
+    {615. / 1372., -270. / 343., 1053. / 1372., 0, 0, 0, 0},
+    {3243. / 5500., -54. / 55., 50949. / 71500., 4998. / 17875., 0, 0, 0},
+    {-26492. / 37125., 72. / 55., 2808. / 23375., -24206. / 37125., 338. / 459., 0, 0},
+    {5561. / 2376., -35. / 11., -24117. / 31603., 899983. / 200772., -5225. / 1836., 3925. / 4056., 0},
+    {465467. / 266112., -2945. / 1232., -5610201. / 14158144., 10513573. / 3212352., -424325. / 205632.,
+     376225. / 454272., 0}};
+static __constant__ double c_dpE[8] = {-13. / 2400., 0., 19683. / 618800., -2401. / 31200., 65. / 816.,
+                                -15. / 416., -521. / 5600., 1. / 10.};
+static __constant__ double c_dpB[8] = {61. / 864., 0., 98415. / 321776., 16807. / 146016., 1375. / 7344.,
+                                1375. / 5408., -37. / 1120., 1. / 10.};
+
+
 // ---------------------------------------------------------------------------
 // Random draws (the reference's curand_uniform_double, replaced by Philox).
 // ---------------------------------------------------------------------------
@@ -48,7 +66,7 @@ __device__ __forceinline__ double start_value(Rng& r, int dist, double range) {
   return sqrt(-log(u1)) * cospi(2.0 * u2);
 }
 
-__device__ void generate_start(Rng& rng, int dist, double range, cd* z /*21*/, cd* q /*30*/) {
+__device__ inline void generate_start(Rng& rng, int dist, double range, cd* z /*21*/, cd* q /*30*/) {
   for (int i = 0; i < 14; ++i) {
     double re = start_value(rng, dist, range);
     double im = start_value(rng, dist, range);
@@ -268,7 +286,7 @@ __device__ __forceinline__ void cognate12(const cd* o, cd P, cd* out) {
 }
 
 // root (21) -> canonical of {root, 1/2 cognate}: the one with the smaller Re(A).
-__device__ void canonical_cognate(const cd* r0, const cd* fpm, cd* out) {
+__device__ inline void canonical_cognate(const cd* r0, const cd* fpm, cd* out) {
   cd r1[NV];
   const cd B = r0[1], F = r0[4], P0 = fpm[0], Pc0 = fpm[8];
   const cd iFB = cinv(F - B);

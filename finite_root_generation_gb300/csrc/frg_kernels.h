@@ -10,6 +10,9 @@
 #ifndef FRG_TRACK_THREADS
 #define FRG_TRACK_THREADS 64
 #endif
+#ifndef FRG_TEAM_THREADS
+#define FRG_TEAM_THREADS 64
+#endif
 
 namespace frg {
 
@@ -19,7 +22,7 @@ struct Handoff {
   cx<double> Yc[23], Vc[23], u[23];
   double s;
   uint64_t rng_index;
-  int streak, step, ministep, tstepQ, n_ivp, n_newton, reason, pad;
+  int streak, step, ministep, tstepQ, n_ivp, n_newton, reason, code;  // reason 6: finished with code
 };
 
 // Device-side arguments of one tracking launch. All arrays are device memory.
@@ -39,7 +42,8 @@ struct TrackArgs {
   cx<double>* yfinal;           // npaths x 23, optional
   double* resid;                // npaths, optional
   int32_t* work;                // npaths x 3 (ivp solves, newton iterations, steps), optional
-  unsigned long long* counters; // 16: codes[8], ivp, newton, steps, -, -, fp64 solves
+  unsigned long long* counters; // 24: codes[8], ivp, newton, steps, fp64 solves, handoffs, -, -,
+                                //     handoff reasons 1..6 at [16..21]
   Handoff* handoff;             // npaths slots (mixed precision)
   int64_t* handoff_list;        // ids of handed-off paths
   unsigned long long* handoff_count;
@@ -50,4 +54,6 @@ struct TrackArgs {
 // mode: 0 plain FP64, 1 FP32 stage with handoff, 2 FP64 resume of handed-off paths
 cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
 cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm);
+cudaError_t frg_launch_team(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
+cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);

@@ -31,23 +31,6 @@
 
 namespace frg {
 
-// Dormand-Prince 6(5) tableau (rungekutta.cu:261-341): stage weights, error
-// weights (LTE, :318-324) and 6th-order solution weights (:334-341).
-__constant__ double c_dpA[8][7] = {
-    {0, 0, 0, 0, 0, 0, 0},
-    {1. / 10., 0, 0, 0, 0, 0, 0},
-    {-2. / 81., 20. / 81., 0, 0, 0, 0, 0},
-    {615. / 1372., -270. / 343., 1053. / 1372., 0, 0, 0, 0},
-    {3243. / 5500., -54. / 55., 50949. / 71500., 4998. / 17875., 0, 0, 0},
-    {-26492. / 37125., 72. / 55., 2808. / 23375., -24206. / 37125., 338. / 459., 0, 0},
-    {5561. / 2376., -35. / 11., -24117. / 31603., 899983. / 200772., -5225. / 1836., 3925. / 4056., 0},
-    {465467. / 266112., -2945. / 1232., -5610201. / 14158144., 10513573. / 3212352., -424325. / 205632.,
-     376225. / 454272., 0}};
-__constant__ double c_dpE[8] = {-13. / 2400., 0., 19683. / 618800., -2401. / 31200., 65. / 816.,
-                                -15. / 416., -521. / 5600., 1. / 10.};
-__constant__ double c_dpB[8] = {61. / 864., 0., 98415. / 321776., 16807. / 146016., 1375. / 7344.,
-                                1375. / 5408., -37. / 1120., 1. / 10.};
-
 enum Phase : int { PH_FETCH = 0, PH_TANGENT0 = 1, PH_RK = 2, PH_NEWTON = 3, PH_SHARP = 4 };
 enum Mode : int { MODE_PLAIN = 0, MODE_LO = 1, MODE_RESUME = 2 };
 
@@ -138,7 +121,8 @@ __device__ void save_handoff(const TrackArgs& a, const PathState<T>& P, int reas
   h.s = double(P.s);
   h.rng_index = P.rng.index;
   h.streak = P.streak; h.step = P.step; h.ministep = P.ministep; h.tstepQ = P.tstepQ;
-  h.n_ivp = P.n_ivp; h.n_newton = P.n_newton; h.reason = reason;
+  h.n_ivp = P.n_ivp; h.n_newton = P.n_newton; h.reason = reason; h.code = 0;
+  if (a.counters) { atomicAdd(&a.counters[12], 1ull); atomicAdd(&a.counters[15 + reason], 1ull); }
   const unsigned long long slot = atomicAdd(a.handoff_count, 1ull);
   a.handoff_list[slot] = P.id;
 }

@@ -1,0 +1,514 @@
+// Warp-cooperative path-tracking kernels: one 8-lane team per path, 4 paths per
+// warp, the linear algebra register-resident (frg_team.cuh) and the path state in
+// shared memory.
+//
+// The control flow is the reference's TrackPath (htpytrack.cu:33-220) with
+// DormandPrince65 (rungekutta.cu:3-123) and Newton (htpysupport.cu:407-494),
+// restated as the same state machine as the one-thread-per-path kernel
+// (frg_track.cu), with identical decisions, tolerances, counters and random draws.
+// Every trip of the loop runs one warp-convergent linear step for all four teams
+// (the expensive part), then each team's control transitions with team-masked
+// shuffles; vector updates are spread over the team's lanes (element e on lane e % 8).
+//
+// Modes as in frg_track.cu: MODE_PLAIN (FP64 from start to root), MODE_LO (FP32
+// stage; every path is handed to the FP64 kernel, either to continue or, when it
+// ended on a step limit, just to be finished), MODE_RESUME (FP64 continuation and
+// finishing of handed-off paths).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "frg_kernels.h"
+#include "frg_team.cuh"
+
+namespace frg {
+namespace team {
+
+enum Phase : int { PH_FETCH = 0, PH_TANGENT0 = 1, PH_RK = 2, PH_NEWTON = 3, PH_SHARP = 4, PH_IDLE = 5 };
+enum Mode : int { MODE_PLAIN = 0, MODE_LO = 1, MODE_RESUME = 2 };
+
+// Draw index of start-value component m (frgkinematics.cu:41-58 order): one draw per
+// uniform value, two per complex-normal component.
+__device__ __forceinline__ double start_component(uint64_t seed, uint64_t stream, int m, int dist, double range) {
+  if (dist == 0) return 2.0 * range * frg_uniform01(seed, stream, (uint64_t)m) - range;
+  const double u1 = frg_uniform01(seed, stream, 2ull * m), u2 = frg_uniform01(seed, stream, 2ull * m + 1);
+  return sqrt(-log(u1)) * cospi(2.0 * u2);
+}
+
+// GenerateStart (frgkinematics.cu:13-136) spread over the team: every lane draws
+// the 14 link values and P0, Pc0; lane g solves the two quadratics of its own j
+// (lane 7 repeats j = 7). Outputs: links z[0..13], U_j, and the lane's parameters
+// P0, Pc0, Pj, Pcj, Qj, Qcj (all FP64).
+__device__ void team_start(uint64_t seed, uint64_t stream, int dist, double range, int j, cd* z, cd& Uj,
+                           cd* sp) {
+#pragma unroll 1
+  for (int i = 0; i < 14; ++i)
+    z[i] = cd(start_component(seed, stream, 2 * i, dist, range), start_component(seed, stream, 2 * i + 1, dist, range));
+  const cd P0(start_component(seed, stream, 28, dist, range), start_component(seed, stream, 29, dist, range));
+  const cd Pc0(start_component(seed, stream, 30, dist, range), start_component(seed, stream, 31, dist, range));
+  const cd Rj(start_component(seed, stream, 32 + 2 * (j - 1), dist, range),
+              start_component(seed, stream, 33 + 2 * (j - 1), dist, range));
+  const uint64_t pmbase = (dist == 0 ? 46ull : 92ull) + 2ull * (j - 1);
+  const cd A = z[0], B = z[1], C = z[2], D = z[3], F = z[4], G = z[5], H = z[6];
+  const cd Ac = z[7], Bc = z[8], Cc = z[9], Dc = z[10], Fc = z[11], Gc = z[12], Hc = z[13];
+  const cd iR = cinv(Rj);
+  cd Aq = (G - D) * (iR * (Hc - Gc) - (Hc - Fc));
+  cd Acq = (Gc - Dc) * (Rj * (H - G) - (H - F));
+  cd Bq = (-(Rj * ((H - G) * (Hc - Fc))) - iR * ((Hc - Gc) * (H - F))) +
+          ((G - D) * (Gc - Dc) + ((H - G) * (Hc - Gc) + ((H - F) * (Hc - Fc) - (F - D) * (Fc - Dc))));
+  double pm = frg_uniform01(seed, stream, pmbase) < 0.5 ? -1.0 : 1.0;
+  cd disc = csqrt_halfangle(Bq * Bq - 4.0 * (Aq * Acq));
+  const cd TUc = cinv(2.0 * Aq) * (-Bq + pm * disc);
+  const cd SUc = cinv(F - D) * (TUc * (G - D) + (Rj * (H - G) - (H - F)));
+  const cd w = (Rj * (H - C) - SUc * (F - B)) - (H - F);
+  const cd wc = (iR * (Hc - Cc) - cinv(SUc) * (Fc - Bc)) - (Hc - Fc);
+  Aq = (Ac - Bc) * w;
+  Acq = (A - B) * wc;
+  Bq = w * wc + ((A - B) * (Ac - Bc) - (C - A) * (Cc - Ac));
+  pm = frg_uniform01(seed, stream, pmbase + 1) < 0.5 ? -1.0 : 1.0;
+  disc = csqrt_halfangle(Bq * Bq - 4.0 * (Aq * Acq));
+  Uj = cinv(2.0 * Aq) * (-Bq + pm * disc);
+  const cd QUc = cdiv(cd(-1.0), C - A) * (cinv(Uj) * (A - B) + w);
+  const cd Qj = QUc * Uj;
+  const cd S = SUc * Uj;
+  sp[0] = P0;
+  sp[1] = Pc0;
+  sp[2] = B + (S * (F - B) + Uj * (P0 - F));
+  sp[3] = Bc + (cinv(S) * (Fc - Bc) + cinv(Uj) * (Pc0 - Fc));
+  sp[4] = Qj;
+  sp[5] = cinv(Qj);
+}
+
+template <typename T> __device__ __forceinline__ const cx<T>* fpm_of(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ const cx<double>* fpm_of<double>(const TrackArgs& a, int task) {
+  return a.fpm + (size_t)task * NP;
+}
+template <> __device__ __forceinline__ const cx<float>* fpm_of<float>(const TrackArgs& a, int task) {
+  return a.fpm_lo + (size_t)task * NP;
+}
+template <typename T> __device__ __forceinline__ cx<T> gamma_of(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ cx<double> gamma_of<double>(const TrackArgs& a, int task) {
+  return a.gamma[task];
+}
+template <> __device__ __forceinline__ cx<float> gamma_of<float>(const TrackArgs& a, int task) {
+  return a.gamma_lo[task];
+}
+
+// Finish a path (FP64, spread over the team): finite check, dehomogenize
+// (frg.cu:44-46, :60), canonical cognate (frgkinematics.cu:227-285, frg.cu:63-65), the
+// row-scaled residual of the target system at the root, outputs and counters.
+__device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, int64_t id, int task, int code,
+                            int g, unsigned tmask, int n_ivp, int n_newton, int steps) {
+  const cd* fpm = a.fpm + (size_t)task * NP;
+  if (a.yfinal)
+    for (int e = g; e < NY; e += TEAM) a.yfinal[(size_t)id * NY + e] = Yf[e];
+  double zl = 0.0;
+  for (int e = g; e < NV; e += TEAM) zl = fmax(zl, sqrt(cnorm2(Yf[e])));
+  const double zmax = team_max(tmask, zl);
+  const cd z0 = Yf[NV];
+  if (code == 0 && a.cfg.inf_tol > 0.0 && sqrt(cnorm2(z0)) < a.cfg.inf_tol * zmax) code = FRG_CODE_INFINITE;
+  // dehomogenized point into S.Ye (SwitchPatch with u = e_21: scale 1/Z0)
+  const cd iz = cdiv(cd(1.0), z0);
+  __syncwarp(tmask);
+  for (int e = g; e < NV; e += TEAM) S.Ye[e] = iz * Yf[e];
+  __syncwarp(tmask);
+  // 1/2 cognate into S.dx: U_down by lane g for j = g + 1, the link sides by lane 0
+  if (g < 7) {
+    const int i = g + 1;
+    const cd B = S.Ye[1], F = S.Ye[4];
+    S.dx[13 + i] = ((fpm[i] - B) - S.Ye[13 + i] * (fpm[0] - F)) * cinv(F - B);
+  }
+  if (g == 0) {
+    cognate12(S.Ye, fpm[0], S.dx);
+    cognate12(S.Ye + 7, fpm[8], S.dx + 7);
+  }
+  __syncwarp(tmask);
+  const bool swap = S.dx[0].re < S.Ye[0].re;
+  cd root_e[3];
+  int ne = 0;
+  for (int e = g; e < NV; e += TEAM) {
+    const cd r = swap ? S.dx[e] : S.Ye[e];
+    a.roots[(size_t)id * NV + e] = r;
+    root_e[ne++] = r;
+  }
+  __syncwarp(tmask);
+  for (int e = g, m = 0; e < NV; e += TEAM, ++m) S.Ye[e] = root_e[m];
+  __syncwarp(tmask);
+  if (a.resid) {
+    // lane g evaluates group j = g + 1 at [root, 1] with q = fpm, dq = 0
+    const int j = g < 7 ? g + 1 : 7;
+    const cd one(1.0), zero(0.0);
+    FrgGroupOut<double> o;
+    const cd* R = S.Ye;
+    frg_group_eval<double>(R[0], R[1], R[2], R[3], R[4], R[5], R[6], R[7], R[8], R[9], R[10], R[11], R[12], R[13],
+                           one, cinv(R[4] - R[1]), cinv(R[6] - R[2]), cinv(R[11] - R[8]), cinv(R[13] - R[9]), one,
+                           one, fpm[0], fpm[8], zero, zero, R[13 + j], cinv(R[13 + j]), fpm[j], fpm[8 + j],
+                           fpm[15 + j], fpm[22 + j], zero, zero, zero, zero, o);
+    double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+    for (int c = 0; c < 8; ++c) m0 = fmax(m0, fmax(fabs(o.dI[c].re), fabs(o.dI[c].im)));
+    for (int c = 0; c < 6; ++c) m1 = fmax(m1, fmax(fabs(o.dII[c].re), fabs(o.dII[c].im)));
+    for (int c = 0; c < 16; ++c) m2 = fmax(m2, fmax(fabs(o.dIII[c].re), fabs(o.dIII[c].im)));
+    double r = fmax(sqrt(cnorm2(o.fI)) / m0, fmax(sqrt(cnorm2(o.fII)) / m1, sqrt(cnorm2(o.fIII)) / m2));
+    r = team_max(tmask, r);
+    if (g == 0) a.resid[id] = r;
+  }
+  if (g == 0) {
+    a.codes[id] = code;
+    if (a.work) {
+      a.work[(size_t)id * 3 + 0] = n_ivp;
+      a.work[(size_t)id * 3 + 1] = n_newton;
+      a.work[(size_t)id * 3 + 2] = steps;
+    }
+    if (a.counters) {
+      atomicAdd(&a.counters[code & 7], 1ull);
+      atomicAdd(&a.counters[8], (unsigned long long)n_ivp);
+      atomicAdd(&a.counters[9], (unsigned long long)n_newton);
+      atomicAdd(&a.counters[10], (unsigned long long)steps);
+    }
+  }
+  __syncwarp(tmask);
+}
+
+template <int MODE, typename T>
+__global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool LO = (MODE == MODE_LO);
+  const unsigned FULL = 0xffffffffu;
+  const frg_config& c = a.cfg;
+  const int lane = threadIdx.x & 31;
+  const int g = lane & 7;
+  const unsigned tmask = 0xffu << (lane & 24);
+  Smem<T>& S = reinterpret_cast<Smem<T>*>(smem_raw)[threadIdx.x >> 3];
+  {
+    cx<T>* base = reinterpret_cast<cx<T>*>(&S);
+    for (int i = g; i < (int)(sizeof(Smem<T>) / sizeof(cx<T>)); i += TEAM) base[i] = cx<T>(T(0));
+  }
+  const T newt_tol = LO ? T(c.newt_tol_lo) : T(c.newt_tol);
+  const int jg = g < 7 ? g + 1 : 7;
+  const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count : a.npaths;
+
+  LaneParams<T> lp;
+  int64_t id = -1;
+  int task = 0;
+  T s = T(0), err = T(0), scale = T(0), residual = T(100);
+  int tstepQ = 0, streak = 0, step = 0, ministep = 0, stage = 0, attempt = 0, it = 0, code = 0;
+  int n_ivp = 0, n_newton = 0;
+  uint64_t rng_index = 0;
+  int phase = PH_FETCH;
+  unsigned long long fp64_solves = 0;
+  __syncwarp();
+
+  for (;;) {
+    // =========================================================== fetch (per team)
+    while (phase == PH_FETCH) {
+      unsigned long long qi = 0;
+      if (g == 0) qi = atomicAdd(a.queue, 1ull);
+      qi = __shfl_sync(tmask, qi, 0, TEAM);
+      if ((int64_t)qi >= nqueue) { phase = PH_IDLE; break; }
+      id = (MODE == MODE_RESUME) ? a.handoff_list[qi] : (int64_t)qi;
+      int lo = 0, hi = a.ntasks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.task_start[mid] <= id) lo = mid; else hi = mid - 1;
+      }
+      task = lo;
+      {
+        cd z[14], Uj, sp[6];
+        team_start(a.seed, (uint64_t)id, c.start_dist, c.start_range, jg, z, Uj, sp);
+        const cx<T>* fpmT = fpm_of<T>(a, task);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) { lp.sp[i] = cx<T>(sp[i]); lp.fp[i] = fpmT[param_index(i, jg)]; }
+        lp.gamma = gamma_of<T>(a, task);
+        if (MODE != MODE_RESUME) {
+          for (int e = g; e < 14; e += TEAM) S.Yc[e] = cx<T>(z[e]);
+          if (g < 7) S.Yc[13 + jg] = cx<T>(Uj);
+          if (g == 7) { S.Yc[21] = cx<T>(T(1)); S.Yc[22] = cx<T>(T(0)); }
+        }
+      }
+      code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
+      if (MODE == MODE_RESUME) {
+        const Handoff& h = a.handoff[id];
+        for (int e = g; e < NY; e += TEAM) {
+          S.Yc[e] = cx<T>(h.Yc[e]); S.Vc[e] = cx<T>(h.Vc[e]); S.u[e] = cx<T>(h.u[e]);
+        }
+        s = T(h.s); rng_index = h.rng_index; streak = h.streak; step = h.step; ministep = h.ministep;
+        tstepQ = h.tstepQ; n_ivp = h.n_ivp; n_newton = h.n_newton;
+        __syncwarp(tmask);
+        if (h.reason == 6) {  // the path already ended on a step limit in the FP32 stage
+          if constexpr (!LO) {
+            cd Yf[NY];
+            for (int e = 0; e < NY; ++e) Yf[e] = h.Yc[e];
+            team_finish(a, *reinterpret_cast<Smem<double>*>(&S), Yf, id, task, h.code, g, tmask, n_ivp, n_newton,
+                        step);
+          }
+          continue;  // next path
+        }
+        phase = PH_RK;
+      } else {
+        __syncwarp(tmask);
+        // TrackPath's patches start at draw 0 of the path's stream (by-value state,
+        // frg.cu:54,57); u (htpytrack.cu:53-58) then the random velocity patch (:63-67).
+        const double R = c.patch_range;
+        for (int e = g; e < NY; e += TEAM) {
+          S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, 2 * e) - R),
+                         T(2.0 * R * frg_uniform01(a.seed, id, 2 * e + 1) - R));
+          S.Vc[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, 46 + 2 * e) - R),
+                          T(2.0 * R * frg_uniform01(a.seed, id, 47 + 2 * e) - R));
+        }
+        rng_index = 92;
+        __syncwarp(tmask);
+        // SwitchPatch(u, Yc, Yc) (htpytrack.cu:60)
+        cx<T> d(T(0));
+        for (int e = g; e < NZ; e += TEAM) d = cfma(S.u[e], S.Yc[e], d);
+        d = cx<T>(team_sum(tmask, d.re), team_sum(tmask, d.im));
+        const cx<T> sc = cdiv(cx<T>(T(1)) - S.u[22] * S.Yc[22], d);
+        __syncwarp(tmask);
+        for (int e = g; e < NZ; e += TEAM) S.Yc[e] = sc * S.Yc[e];
+        s = T(c.s_init); tstepQ = 0; streak = c.caution_steps - 1; step = 0; ministep = 0;
+        n_ivp = 0; n_newton = 0;
+        phase = PH_TANGENT0;
+      }
+    }
+    if (__all_sync(FULL, phase == PH_IDLE)) break;
+
+    // ==================================================== set up (per team)
+    const bool newton = (phase == PH_NEWTON || phase == PH_SHARP);
+    bool tstep = false;
+    T tgoal = T(0);
+    const cx<T>* Wsrc = S.Vc;
+    cx<T>* dst = S.dx;
+    if (phase == PH_TANGENT0 || phase == PH_IDLE) {
+      for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.Yc[e];
+    } else if (phase == PH_RK) {
+      tstep = tstepQ != 0;
+      dst = S.k[stage];
+      if (stage == 0) {
+        for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.Yc[e];
+      } else {
+        Wsrc = S.k[stage - 1];
+        const double* w = c_dpA[stage];
+        for (int e = g; e < NY; e += TEAM) {
+          cx<T> acc = T(w[stage - 1]) * s * S.k[stage - 1][e];
+          for (int l = stage - 2; l >= 0; --l) acc = T(w[l]) * s * S.k[l][e] + acc;
+          S.Ye[e] = S.Yc[e] + acc;
+        }
+      }
+    } else {
+      tgoal = (phase == PH_SHARP) ? T(1) : S.Yn[22].re;
+      for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.YN[e];
+    }
+    __syncwarp();
+
+    // ========================================== linear step (whole warp)
+    const StepOut<T> r = linear_step<T>(S, Wsrc, dst, newton, tstep, tgoal, lp, g);
+    __syncwarp();
+    if (phase == PH_IDLE) continue;
+    if (!LO) ++fp64_solves;
+    if (newton) ++n_newton; else ++n_ivp;
+
+    // ============================================= transitions (per team)
+    bool finished = false;
+    int handoff = 0;
+    bool final_from_YN = false;
+    if (LO && !(r.ratio <= T(c.cond_switch))) {
+      handoff = 2;  // ill-conditioned (or non-finite) step: continue in FP64 from Yc
+    } else if (phase == PH_TANGENT0) {
+      for (int e = g; e < NY; e += TEAM) S.Vc[e] = S.dx[e];
+      if (c.max_steps == 0) { code = 1; finished = true; }
+      stage = 0;
+      phase = PH_RK;
+    } else if (phase == PH_RK) {
+      if (++stage == 8) {
+        stage = 0;
+        // error estimate and step factor (rungekutta.cu:317-331), prediction (:333-341)
+        T es = T(0);
+        for (int e = g; e < NY; e += TEAM) {
+          cx<T> le = T(c_dpE[7]) * s * S.k[7][e];
+          cx<T> yb = T(c_dpB[7]) * s * S.k[7][e];
+          for (int l = 6; l >= 0; --l) {
+            if (c_dpE[l] != 0.0) le = T(c_dpE[l]) * s * S.k[l][e] + le;
+            if (c_dpB[l] != 0.0) yb = T(c_dpB[l]) * s * S.k[l][e] + yb;
+          }
+          es += cnorm2(le);
+          S.Yn[e] = S.Yc[e] + yb;
+          S.Vn[e] = S.k[7][e];
+        }
+        err = sqrt(team_sum(tmask, es));
+        scale = (err > T(10e-17)) ? T(0.8) * pow(T(c.rk_tol) / err, T(1) / T(6)) : T(5);
+        if (scale > T(5)) scale = T(5);
+        __syncwarp(tmask);
+        if (ministep++ == c.max_ministeps) { code = 2; finished = true; }
+        else if (err <= T(c.rk_tol)) {
+          const T tn = S.Yn[22].re;
+          if (LO && tn > T(1.0 - c.nudge_trigger)) handoff = 5;  // the endgame runs in FP64
+          else if (tn <= T(1.0 - c.nudge_trigger)) { attempt = 0; phase = PH_NEWTON; }
+          else if (fabs(T(1) - tn) < T(c.sharp_trigger)) { attempt = 0; phase = PH_SHARP; }
+          else { tstepQ = 1; s = T(1) - S.Yc[22].re; }  // land on t = 1 (htpytrack.cu:120-123)
+          if (phase == PH_NEWTON || phase == PH_SHARP) {
+            for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+            residual = T(100);
+            it = 0;
+          }
+        } else if (s <= T(c.s_min)) {
+          if (LO) handoff = 4; else { code = 3; finished = true; }
+        } else {
+          s *= scale;
+          if (s < T(c.s_min)) s = T(c.s_min * 0.9);
+          streak = 0;
+        }
+      }
+    } else {
+      // one corrector or sharpening iteration (htpysupport.cu:427-492)
+      const bool sharp = (phase == PH_SHARP);
+      const int max_its = sharp ? c.sharp_its : c.newt_its;
+      const T tol = sharp ? T(c.sharp_tol) : newt_tol;
+      const int restype = sharp ? c.sharp_residual : c.newt_residual;
+      bool done = false;
+      if (restype == 0 && it > 0) {
+        residual = r.hnorm;  // |H| at the current point: the residual of the previous update
+        if (!(it < max_its && residual > tol)) done = true;
+      }
+      if (!done) {
+        for (int e = g; e < NY; e += TEAM) S.YN[e] += S.dx[e];
+        it++;
+        if (restype != 0) {
+          residual = sqrt(r.xnorm2);
+          if (!(it < max_its && residual > tol)) done = true;
+        }
+      }
+      __syncwarp(tmask);
+      if (done) {
+        const bool ok = residual < (sharp ? T(c.sharp_tol) : newt_tol);
+        if (ministep++ == c.max_ministeps) { code = 2; finished = true; final_from_YN = sharp; }
+        else if (ok && !sharp) {
+          if (fabs(T(1) - S.Yn[22].re) < T(c.sharp_trigger)) {
+            attempt = 0; phase = PH_SHARP;
+            for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+            residual = T(100); it = 0;
+          } else {
+            // accept the step (htpytrack.cu:176-183)
+            for (int e = g; e < NY; e += TEAM) { S.Yc[e] = S.YN[e]; S.Vc[e] = S.Vn[e]; }
+            streak++;
+            if (streak < c.caution_steps && scale > T(1)) scale = T(1);
+            s *= scale;
+            if (s > T(c.s_max)) s = T(c.s_max);
+            else if (s < T(c.s_min)) s = T(c.s_min * 0.9);
+            step++;
+            if (step == c.max_steps) { code = 1; finished = true; }
+            else if (LO && S.YN[22].re >= T(c.t_switch)) handoff = 1;
+            else { stage = 0; phase = PH_RK; }
+          }
+        } else if (ok && sharp) {
+          code = 0; finished = true; final_from_YN = true;
+        } else {
+          // new random patch and SwitchPatch(u, Yn, Yn) (htpytrack.cu:145-151, :204-210)
+          const double R = c.patch_range;
+          for (int e = g; e < NY; e += TEAM)
+            S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, rng_index + 2 * e) - R),
+                           T(2.0 * R * frg_uniform01(a.seed, id, rng_index + 2 * e + 1) - R));
+          rng_index += 46;
+          __syncwarp(tmask);
+          cx<T> d(T(0));
+          for (int e = g; e < NZ; e += TEAM) d = cfma(S.u[e], S.Yn[e], d);
+          d = cx<T>(team_sum(tmask, d.re), team_sum(tmask, d.im));
+          const cx<T> sc = cdiv(cx<T>(T(1)) - S.u[22] * S.Yn[22], d);
+          __syncwarp(tmask);
+          for (int e = g; e < NZ; e += TEAM) S.Yn[e] = sc * S.Yn[e];
+          if (!sharp) {
+            if (++attempt < c.newt_attempts) {
+              for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+              residual = T(100); it = 0;
+            } else if (s <= T(c.s_min)) {
+              if (LO) handoff = 3; else { code = 4; finished = true; }
+            } else {
+              s *= T(0.5);
+              if (s < T(c.s_min)) s = T(c.s_min * 0.9);
+              streak = 0;
+              stage = 0;
+              phase = PH_RK;
+            }
+          } else {
+            if (++attempt < c.sharp_attempts) {
+              for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+              residual = T(100); it = 0;
+            } else {
+              code = 5; finished = true; final_from_YN = true;
+            }
+          }
+        }
+      }
+    }
+    __syncwarp(tmask);
+
+    if (LO && (handoff || finished)) {
+      // save the state for the FP64 kernel (always: an FP32 path is finished in FP64)
+      Handoff& h = a.handoff[id];
+      for (int e = g; e < NY; e += TEAM) { h.Yc[e] = cd(S.Yc[e]); h.Vc[e] = cd(S.Vc[e]); h.u[e] = cd(S.u[e]); }
+      if (g == 0) {
+        h.s = double(s); h.rng_index = rng_index; h.streak = streak; h.step = step; h.ministep = ministep;
+        h.tstepQ = tstepQ; h.n_ivp = n_ivp; h.n_newton = n_newton;
+        h.reason = finished ? 6 : handoff; h.code = code;
+        if (a.counters) {
+          if (!finished) atomicAdd(&a.counters[12], 1ull);
+          atomicAdd(&a.counters[15 + (finished ? 6 : handoff)], 1ull);
+        }
+        const unsigned long long slot = atomicAdd(a.handoff_count, 1ull);
+        a.handoff_list[slot] = id;
+      }
+      __syncwarp(tmask);
+      phase = PH_FETCH;
+      continue;
+    }
+    if (finished) {
+      if constexpr (!LO) {
+        cd Yf[NY];
+        const cx<T>* src = final_from_YN ? S.YN : S.Yc;
+        for (int e = 0; e < NY; ++e) Yf[e] = cd(src[e]);
+        __syncwarp(tmask);
+        team_finish(a, S, Yf, id, task, code, g, tmask, n_ivp, n_newton, step);
+      }
+      phase = PH_FETCH;
+    }
+  }
+  if (a.counters && fp64_solves && g == 0) atomicAdd(&a.counters[11], fp64_solves);
+}
+
+}  // namespace team
+}  // namespace frg
+
+namespace {
+template <int MODE, typename T>
+cudaError_t team_launch(const frg::TrackArgs& args, int grid, cudaStream_t stream) {
+  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T>);
+  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  frg::team::team_kernel<MODE, T><<<grid, FRG_TEAM_THREADS, smem, stream>>>(args);
+  return cudaGetLastError();
+}
+template <int MODE, typename T>
+cudaError_t team_occ(int* bps) {
+  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T>);
+  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, frg::team::team_kernel<MODE, T>, FRG_TEAM_THREADS, smem);
+}
+}  // namespace
+
+cudaError_t frg_launch_team(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream) {
+  switch (mode) {
+    case 0: return team_launch<frg::team::MODE_PLAIN, double>(args, grid, stream);
+    case 1: return team_launch<frg::team::MODE_LO, float>(args, grid, stream);
+    case 2: return team_launch<frg::team::MODE_RESUME, double>(args, grid, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm) {
+  switch (mode) {
+    case 0: return team_occ<frg::team::MODE_PLAIN, double>(blocks_per_sm);
+    case 1: return team_occ<frg::team::MODE_LO, float>(blocks_per_sm);
+    case 2: return team_occ<frg::team::MODE_RESUME, double>(blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+  }
+}

@@ -56,6 +56,7 @@ enum { FRG_CODE_OK = 0, FRG_CODE_MAX_STEPS = 1, FRG_CODE_MAX_MINISTEPS = 2, FRG_
 enum { FRG_PREC_FP64 = 0, FRG_PREC_MIXED = 1 };
 enum { FRG_START_UNIFORM = 0, FRG_START_NORMAL = 1 };
 enum { FRG_GAMMA_FIXED = 0, FRG_GAMMA_RANDOM = 1 };
+enum { FRG_KERNEL_TEAM = 0, FRG_KERNEL_THREAD = 1 };
 
 /* Run configuration. frg_config_default() fills the reference's compile-time
  * constants: tracker settings htpytrack.cu:9-31, start range frgkinematics.cu:7-8,
@@ -86,6 +87,7 @@ typedef struct frg_config {
   int threads_per_block; /* 0 = tuned default */
   int blocks_per_sm;     /* 0 = tuned default */
   double newt_tol_lo;    /* mixed: corrector tolerance of the FP32 stage */
+  int kernel_variant;    /* FRG_KERNEL_TEAM (8 lanes per path, default) or FRG_KERNEL_THREAD */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */
@@ -99,6 +101,9 @@ typedef struct frg_stats {
   double track_ms;         /* device time of the tracking kernel(s) */
   double total_ms;         /* wall time of the call, copies included */
   int64_t handoffs;        /* mixed precision: paths continued in FP64 */
+  double stage_ms[2];      /* device time of the FP32 stage and of the FP64 kernel */
+  int64_t handoff_reason[6]; /* mixed: t_switch, ill-conditioned, corrector at s_min,
+                                predictor at s_min, endgame entry, ended on a step limit */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;

@@ -15,10 +15,11 @@ pytestmark = pytest.mark.gpu
 ROOT_RTOL = 1e-8
 
 
-@pytest.fixture(scope="module")
-def tracker():
+@pytest.fixture(scope="module", params=[frg.KERNEL_TEAM, frg.KERNEL_THREAD], ids=["team", "thread"])
+def tracker(request):
     frg_build.build()
-    t = frg.Tracker()
+    t = frg.Tracker(frg.default_config(kernel_variant=request.param))
+    t.variant = request.param
     yield t
     t.close()
 
@@ -33,10 +34,17 @@ def test_reference_paths_path_for_path(tracker, golden):
     n = len(golden["path_codes"])
     res = tracker.track(REFERENCE_TARGET, [n], seed, want_yfinal=True, want_resid=True)
     want = golden["path_codes"]
-    assert np.array_equal(res.codes, want)
     ok = want == 0
-    assert np.all(_rel(res.roots[ok], golden["path_roots"][ok]) < ROOT_RTOL)
-    assert np.all(res.resid[ok] <= 1e-10)
+    if tracker.variant == frg.KERNEL_THREAD:
+        # the reference's dense LU restated: same codes everywhere
+        assert np.array_equal(res.codes, want)
+        assert np.all(_rel(res.roots[ok], golden["path_roots"][ok]) < ROOT_RTOL)
+    else:
+        # structured elimination: rounding differs, the tracked roots do not
+        same = (res.codes[ok] == 0) & (_rel(res.roots[ok], golden["path_roots"][ok]) < ROOT_RTOL)
+        assert same.mean() >= 0.99
+        assert (res.codes == want).mean() >= 0.97
+    assert np.all(res.resid[res.codes == 0] <= 1e-10)
 
 
 def test_random_task_matches_oracle(tracker, oracle):
@@ -92,16 +100,21 @@ def test_deterministic(tracker):
 def test_empty_and_limits(tracker):
     r = tracker.track(REFERENCE_TARGET, [0], 1)
     assert r.roots.shape == (0, 21) and r.stats["paths"] == 0
-    t = frg.Tracker(frg.default_config(max_steps=0))
+    v = tracker.variant
+    t = frg.Tracker(frg.default_config(max_steps=0, kernel_variant=v))
     assert np.all(t.track(REFERENCE_TARGET, [16], 1).codes == 1)
-    t.set_config(frg.default_config(max_ministeps=3))
+    t.set_config(frg.default_config(max_ministeps=3, kernel_variant=v))
     assert np.all(t.track(REFERENCE_TARGET, [16], 1).codes == 2)
+    for prec in (frg.PREC_MIXED,):
+        t.set_config(frg.default_config(max_ministeps=3, kernel_variant=v, precision=prec))
+        assert np.all(t.track(REFERENCE_TARGET, [16], 1).codes == 2)
     t.close()
 
 
 def test_oracle_config_knobs_match(tracker, oracle):
     """Non-default tracker settings (residual type |H|, normal starts) still match the oracle."""
-    cfg = frg.default_config(newt_residual=0, start_dist=frg.START_NORMAL, start_range=1.0)
+    cfg = frg.default_config(newt_residual=0, start_dist=frg.START_NORMAL, start_range=1.0,
+                             kernel_variant=tracker.variant)
     t = frg.Tracker(cfg)
     n = 96
     res = t.track(REFERENCE_TARGET, [n], 3)
@@ -119,3 +132,18 @@ def test_stats_counters(tracker):
     assert s["paths"] == 64 and sum(s["codes"]) == 64
     assert np.bincount(res.codes, minlength=8).tolist() == s["codes"]
     assert s["ivp_solves"] > 64 * 100 and s["newton_iters"] > 0 and s["track_ms"] > 0
+
+
+def test_team_matches_thread_kernel():
+    """The two FP64 kernels (dense LU per thread, structured LU per 8-lane team)
+    track the same paths to the same roots."""
+    fpm = precision_point_task(12, "disk")
+    n = 512
+    with frg.Tracker(frg.default_config(kernel_variant=frg.KERNEL_THREAD)) as t:
+        a = t.track(fpm, [n], 31, want_resid=True)
+    with frg.Tracker(frg.default_config(kernel_variant=frg.KERNEL_TEAM)) as t:
+        b = t.track(fpm, [n], 31, want_resid=True)
+    ok = a.codes == 0
+    same = (b.codes[ok] == 0) & (_rel(b.roots[ok], a.roots[ok]) < ROOT_RTOL)
+    assert same.mean() >= 0.99
+    assert np.all(b.resid[b.codes == 0] <= 1e-10)
