@@ -83,7 +83,9 @@ EXPORTS = [
     "frg_config_default", "frg_create", "frg_destroy", "frg_last_error", "frg_set_config", "frg_track",
     "frg_track_async", "frg_coll_create", "frg_coll_destroy", "frg_coll_size", "frg_coll_get", "frg_coll_merge",
     "frg_coll_save", "frg_coll_load", "frg_codes_append", "frg_lambertw0", "frg_estimate_collected",
+    "frg_track_noalloc",
 ]
+NOALLOC_MAX_TASKS = 1024
 
 _lib = None
 
@@ -121,6 +123,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_coll_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.frg_coll_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.frg_codes_append.argtypes = [ctypes.c_char_p, _I32, ctypes.c_int64]
+    lib.frg_track_noalloc.argtypes = [ctypes.POINTER(FrgConfig), ctypes.c_void_p, ctypes.c_int, _I64,
+                                      ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
     _lib = lib
     return lib
 

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfrg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["frg_track.cu", "frg_track_team.cu", "frg_capi.cu"]
+CUDA_SOURCES = ["frg_track.cu", "frg_track_team.cu", "frg_capi.cu", "frg_noalloc.cu"]
 CXX_SOURCES = ["frg_collect.cpp"]
 
 

@@ -140,6 +140,25 @@ frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const in
                            uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
                            void* stream);
 
+/* Plain FP64 tracking that allocates no device memory. No counterpart in the
+ * reference: it is for callers that may not call cudaMalloc / cudaFree, such as code
+ * hosted in a framework that owns all device memory through its own pool, or loops
+ * that cannot afford cudaFree's device-wide synchronisation. The caller passes device
+ * buffers for fpm, roots, codes and (optional) resid; cfg and paths_per_task are host
+ * memory; cfg->precision must be FRG_PREC_FP64. The work runs on the current device,
+ * enqueued on `stream` (a cudaStream_t, NULL for the legacy stream); the call returns
+ * before it completes. The kernels' scratch (queue head, counters, per-task gamma and
+ * path offsets) is a static device array of FRG_NOALLOC_SCRATCH_BYTES kept by every
+ * GPU that loads the library until exit, so a call takes at most
+ * FRG_NOALLOC_MAX_TASKS tasks (more returns FRG_ERR_ARG). The first call on a device
+ * looks up the array's device address; make it before any stream capture. All calls
+ * share the array: calls whose GPU work overlaps on one device race. Errors are
+ * reported by the status alone (FRG_ERR_ARG for bad arguments, FRG_ERR_CUDA). */
+#define FRG_NOALLOC_MAX_TASKS 1024
+#define FRG_NOALLOC_SCRATCH_BYTES 32768
+frg_status frg_track_noalloc(const frg_config* cfg, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                             uint64_t seed, double* roots, int32_t* codes, double* resid, void* stream);
+
 /* ---- root collection (replaces SortingDeletingMerging, frgsupport.cu:10-215, and
  *      the thrust ordering of frg.cu:432-435) ---- */
 typedef struct frg_coll frg_coll;
