@@ -209,20 +209,31 @@ def flops_per_solve():
 
 
 # ---------------------------------------------------------------------- our impl
-def _track_steps(frg, torch, tracker, task, n, seeds, bufs, flush):
-    """Run one step per seed into device buffers; returns per-step stats and the
-    distinct finite roots of each step (computed on the host after the timed kernels)."""
-    d_fpm, d_roots, d_codes, d_resid = bufs
-    stats, sets = [], []
-    for sd in seeds:
+def _timed_steps(torch, tracker, n, seeds, d_fpm, outs, flush, world):
+    """Run one step per seed, step i writing into outs[i] (device buffers), timed as one
+    region with CUDA events bracketed by a barrier and a synchronize on both sides.
+    L2 is flushed (a 256 MB write) before every step. Returns (ms, per-step stats)."""
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    stats = []
+    for sd, (roots, codes, resid) in zip(seeds, outs):
         flush.zero_()
-        torch.cuda.synchronize()
-        st = tracker.track_into(d_fpm, [n], sd, d_roots, d_codes, resid=d_resid)
-        stats.append(st)
-        roots = d_roots.cpu().numpy().view(np.complex128)
-        from finite_root_generation_gb300.metrics import distinct_roots
-        sets.append(distinct_roots(roots, d_codes.cpu().numpy(), d_resid.cpu().numpy(), RESID_MAX))
-    return stats, sets
+        stats.append(tracker.track_into(d_fpm, [n], sd, roots, codes, resid=resid))
+    ev1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    return ev0.elapsed_time(ev1), stats
+
+
+def _distinct_sets(outs):
+    from finite_root_generation_gb300.metrics import distinct_roots
+    return [distinct_roots(r.cpu().numpy().view(np.complex128), c.cpu().numpy(), e.cpu().numpy(), RESID_MAX)
+            for r, c, e in outs]
 
 
 def run_ours(args, rank, world):
@@ -240,31 +251,35 @@ def run_ours(args, rank, world):
     n = args.paths
     chosen = frg.Tracker(workload_config(frg, frg.PREC_MIXED), device=dev)
     plain = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
-    bufs = (torch.from_numpy(task.view(np.float64).copy()).cuda(),
-            torch.empty((n, 42), dtype=torch.float64, device="cuda"),
-            torch.empty(n, dtype=torch.int32, device="cuda"),
-            torch.empty(n, dtype=torch.float64, device="cuda"))
+    d_fpm = torch.from_numpy(task.view(np.float64).copy()).cuda()
+
+    def out_bufs(k):
+        return [(torch.empty((n, 42), dtype=torch.float64, device="cuda"),
+                 torch.empty(n, dtype=torch.int32, device="cuda"),
+                 torch.empty(n, dtype=torch.float64, device="cuda")) for _ in range(k)]
+
+    outs = out_bufs(args.steps)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def seed_of(step):
         return 1000003 * (rank + 1) + step
 
     for w in range(args.warmup):
-        chosen.track_into(bufs[0], [n], seed_of(-1 - w), bufs[1], bufs[2], resid=bufs[3])
-    plain.track_into(bufs[0], [min(n, 8192)], seed_of(-1), bufs[1], bufs[2], resid=bufs[3])
+        chosen.track_into(d_fpm, [n], seed_of(-1 - w), *outs[0][:2], resid=outs[0][2])
+    plain.track_into(d_fpm, [min(n, 8192)], seed_of(-1), *outs[0][:2], resid=outs[0][2])
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
 
-    # ---- chosen configuration, device-resident (value) ----
+    # ---- chosen configuration, inputs resident in HBM (value) ----
     seeds = [seed_of(k) for k in range(args.steps)]
     with ClockSampler(dev) as clk:
-        c_stats, c_sets = _track_steps(frg, torch, chosen, task, n, seeds, bufs, flush)
-    torch.cuda.synchronize()
+        track_ms, c_stats = _timed_steps(torch, chosen, n, seeds, d_fpm, outs, flush, world)
     clocks = clk.summary()
+    c_sets = _distinct_sets(outs)
     # ---- plain FP64 on the same seeds (ratio and recall) ----
     p_seeds = seeds[: max(1, args.plain_steps)]
-    p_stats, p_sets = _track_steps(frg, torch, plain, task, n, p_seeds, bufs, flush)
+    p_outs = outs[: len(p_seeds)]
+    p_ms, p_stats = _timed_steps(torch, plain, n, p_seeds, d_fpm, p_outs, flush, world)
+    p_sets = _distinct_sets(p_outs)
     rec = [recall(p_sets[i], c_sets[i]) for i in range(len(p_seeds))]
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
@@ -282,9 +297,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
-    track_ms = sum(st["track_ms"] for st in c_stats)
     distinct = sum(len(d) for d in c_sets)
-    p_ms = sum(st["track_ms"] for st in p_stats)
     p_distinct = sum(len(d) for d in p_sets)
     t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct], dtype=torch.float64)
     if world > 1:
@@ -293,6 +306,7 @@ def run_ours(args, rank, world):
         torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
         track_ms, e2e_s, p_ms = float(tmax[0]), float(tmax[1]), float(tmax[4])
         distinct, e2e_distinct, p_distinct = float(tsum[2]), float(tsum[3]), float(tsum[5])
+    chosen_rounds = chosen.config.mixed_rounds
     chosen.close()
     plain.close()
     if rank != 0:
@@ -353,7 +367,9 @@ def run_ours(args, rank, world):
                      "flops_per_solve": fps,
                      "kernels": {kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
                                  for kk, v in kernels.items()}},
-        "gpu_launches": 3 * k,
+        # per step: two conversions of the task parameters (FP32, double-float), then
+        # per mixed round one FP32-stage and one FP64-stage tracking kernel
+        "gpu_launches": (2 + 2 * max(1, chosen_rounds)) * k,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -398,7 +414,8 @@ def cpu_baseline(args, sample_paths=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    cb = cpu_baseline(args, sample_paths=args.cpu_sample)
+    for _ in range(max(1, args.warmup)):
+        cb = cpu_baseline(args, sample_paths=args.cpu_sample)
     t0 = time.perf_counter()
     vals = []
     for _ in range(args.steps):
@@ -425,7 +442,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--paths", type=int, default=65536)
-    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--cpu-sample", type=int, default=8192)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")

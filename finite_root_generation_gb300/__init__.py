@@ -58,6 +58,7 @@ class FrgConfig(ctypes.Structure):
         ("inf_tol", ctypes.c_double),
         ("threads_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
         ("newt_tol_lo", ctypes.c_double), ("kernel_variant", ctypes.c_int),
+        ("mixed_rounds", ctypes.c_int), ("lo_refine", ctypes.c_int), ("lo_endgame", ctypes.c_int),
     ]
 
 
@@ -69,13 +70,15 @@ class FrgStats(ctypes.Structure):
         ("newton_iters", ctypes.c_int64), ("fp64_solves", ctypes.c_int64), ("steps", ctypes.c_int64),
         ("track_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("handoffs", ctypes.c_int64),
         ("stage_ms", ctypes.c_double * 2), ("handoff_reason", ctypes.c_int64 * 6),
+        ("kernel_cycles", ctypes.c_int64 * 12), ("handbacks", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
         return {"paths": self.paths, "codes": list(self.codes), "ivp_solves": self.ivp_solves,
                 "newton_iters": self.newton_iters, "fp64_solves": self.fp64_solves, "steps": self.steps,
                 "track_ms": self.track_ms, "total_ms": self.total_ms, "handoffs": self.handoffs,
-                "stage_ms": list(self.stage_ms), "handoff_reason": list(self.handoff_reason)}
+                "stage_ms": list(self.stage_ms), "handoff_reason": list(self.handoff_reason),
+                "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.

@@ -56,8 +56,10 @@ struct frg_ctx {
   int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each thread-per-path kernel mode
   int team_blocks_per_sm[3] = {0, 0, 0};
   std::string err;
-  DevBuf fpm, gamma, fpm_lo, gamma_lo, task_start, queue, counters, roots, codes, yfinal, resid;
-  DevBuf handoff, handoff_list;
+  DevBuf fpm, gamma, fpm_lo, gamma_lo, fpm_df, gamma_df, task_start, queue, counters, roots, codes, yfinal, resid;
+  DevBuf handoff, handoff_list, lo_lists;
+  std::vector<cudaEvent_t> round_ev;  // events around the mixed-precision launches
+  int last_rounds = 0;
 };
 
 static frg_status fail(frg_ctx* ctx, frg_status s, const std::string& msg) {
@@ -94,11 +96,15 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->dup_tol = 1e-6;
   c->precision = FRG_PREC_FP64;
   c->t_switch = 0.99;
-  c->cond_switch = 1e6;
+  c->cond_switch = 1e5;
   c->inf_tol = 0.0;
   c->threads_per_block = 0;
   c->blocks_per_sm = 0;
   c->newt_tol_lo = 1e-5;
+  c->kernel_variant = FRG_KERNEL_TEAM;
+  c->mixed_rounds = 1;
+  c->lo_refine = 1;
+  c->lo_endgame = 0;
   return FRG_OK;
 }
 
@@ -117,6 +123,7 @@ static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
     return fail(ctx, FRG_ERR_ARG, "unknown precision");
   if (c->kernel_variant != FRG_KERNEL_TEAM && c->kernel_variant != FRG_KERNEL_THREAD)
     return fail(ctx, FRG_ERR_ARG, "unknown kernel_variant");
+  if (c->mixed_rounds < 0 || c->mixed_rounds > 64) return fail(ctx, FRG_ERR_ARG, "mixed_rounds must be in 0..64");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   return FRG_OK;
@@ -157,12 +164,14 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->task_start, &ctx->queue,
+  for (DevBuf* b : {&ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->fpm_df, &ctx->gamma_df,
+                    &ctx->task_start, &ctx->queue,
                     &ctx->counters, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->handoff,
-                    &ctx->handoff_list})
+                    &ctx->handoff_list, &ctx->lo_lists})
     b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (cudaEvent_t e : ctx->round_ev) cudaEventDestroy(e);
   if (ctx->evmid) cudaEventDestroy(ctx->evmid);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -200,23 +209,31 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   std::vector<cx<double>> g;
   task_gammas(ctx->cfg, seed, ntasks, g);
   std::vector<cx<float>> g_lo(ntasks);
-  for (int k = 0; k < ntasks; ++k) g_lo[k] = cx<float>(g[k]);
+  std::vector<cx<df>> g_df(ntasks);
+  for (int k = 0; k < ntasks; ++k) {
+    g_lo[k] = cx<float>(g[k]);
+    g_df[k] = cx<df>(df(g[k].re), df(g[k].im));
+  }
   std::vector<int64_t> starts(ntasks + 1, 0);
   for (int k = 0; k < ntasks; ++k) starts[k + 1] = starts[k] + ppt[k];
   FRG_CUDA(ctx, ctx->gamma.ensure(sizeof(cx<double>) * ntasks));
   FRG_CUDA(ctx, ctx->gamma_lo.ensure(sizeof(cx<float>) * ntasks));
   FRG_CUDA(ctx, ctx->fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, ctx->fpm_df.ensure(sizeof(cx<df>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, ctx->gamma_df.ensure(sizeof(cx<df>) * ntasks));
+  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_df.p, g_df.data(), sizeof(cx<df>) * ntasks, cudaMemcpyHostToDevice, st));
   FRG_CUDA(ctx, ctx->task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
-  FRG_CUDA(ctx, ctx->queue.ensure(sizeof(unsigned long long) * 4));
-  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 24));
+  FRG_CUDA(ctx, ctx->queue.ensure(sizeof(unsigned long long) * 8));
+  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 40));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma.p, g.data(), sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_lo.p, g_lo.data(), sizeof(cx<float>) * ntasks, cudaMemcpyHostToDevice,
                                 st));
   FRG_CUDA(ctx, cudaMemcpyAsync(ctx->task_start.p, starts.data(), sizeof(int64_t) * (ntasks + 1),
                                 cudaMemcpyHostToDevice, st));
-  FRG_CUDA(ctx, cudaMemsetAsync(ctx->queue.p, 0, sizeof(unsigned long long) * 4, st));
-  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 24, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(ctx->queue.p, 0, sizeof(unsigned long long) * 8, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 40, st));
   FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)ctx->fpm_lo.p, FRG_NP * ntasks, st));
+  FRG_CUDA(ctx, frg_launch_to_df(d_fpm, (cx<df>*)ctx->fpm_df.p, FRG_NP * ntasks, st));
 
   frg::TrackArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -225,6 +242,8 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   a.gamma = (const cx<double>*)ctx->gamma.p;
   a.fpm_lo = (const cx<float>*)ctx->fpm_lo.p;
   a.gamma_lo = (const cx<float>*)ctx->gamma_lo.p;
+  a.fpm_df = (const cx<df>*)ctx->fpm_df.p;
+  a.gamma_df = (const cx<df>*)ctx->gamma_df.p;
   a.task_start = (const int64_t*)ctx->task_start.p;
   a.ntasks = ntasks;
   a.npaths = N;
@@ -257,18 +276,47 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
     if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64)");
     return FRG_OK;
   }
+  // Rounds of (FP32 kernel, FP64 kernel). The FP64 kernel hands paths that are well
+  // conditioned again (and before t_switch) back to the next round's FP32 kernel; the
+  // last round keeps every path in FP64 until it ends. Queue heads and counts live in
+  // q: [0] FP32 queue, [1] FP64 queue, [2] FP64 list count, [3], [4] hand-back counts.
   FRG_CUDA(ctx, ctx->handoff.ensure(sizeof(frg::Handoff) * (size_t)N));
   FRG_CUDA(ctx, ctx->handoff_list.ensure(sizeof(int64_t) * (size_t)N));
+  FRG_CUDA(ctx, ctx->lo_lists.ensure(sizeof(int64_t) * 2 * (size_t)N));
   a.handoff = (frg::Handoff*)ctx->handoff.p;
   a.handoff_list = (int64_t*)ctx->handoff_list.p;
   a.handoff_count = q + 2;
-  a.queue = q;
-  cudaError_t e = launch(1, grid_for(1, N));
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
-  FRG_CUDA(ctx, cudaEventRecord(ctx->evmid, st));
-  a.queue = q + 1;
-  e = launch(2, grid_for(2, N));
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
+  int64_t* lo = (int64_t*)ctx->lo_lists.p;
+  const int rounds = team ? (ctx->cfg.mixed_rounds > 0 ? ctx->cfg.mixed_rounds : 1) : 1;
+  if ((int)ctx->round_ev.size() < 2 * rounds + 1) {
+    while ((int)ctx->round_ev.size() < 2 * rounds + 1) {
+      cudaEvent_t ev;
+      FRG_CUDA(ctx, cudaEventCreate(&ev));
+      ctx->round_ev.push_back(ev);
+    }
+  }
+  FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[0], st));
+  for (int r = 0; r < rounds; ++r) {
+    if (r > 0) FRG_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned long long) * 3, st));
+    FRG_CUDA(ctx, cudaMemsetAsync(q + 3 + (r & 1), 0, sizeof(unsigned long long), st));
+    a.queue = q;
+    a.lo_list = r == 0 ? nullptr : lo + (size_t)((r - 1) & 1) * N;
+    a.lo_count = r == 0 ? nullptr : q + 3 + ((r - 1) & 1);
+    a.back_list = nullptr;
+    a.back_count = nullptr;
+    cudaError_t e = launch(1, grid_for(1, N));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
+    FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[2 * r + 1], st));
+    a.queue = q + 1;
+    a.lo_list = nullptr;
+    a.lo_count = nullptr;
+    a.back_list = (team && r + 1 < rounds) ? lo + (size_t)(r & 1) * N : nullptr;
+    a.back_count = q + 3 + (r & 1);
+    e = launch(2, grid_for(2, N));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
+    FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[2 * r + 2], st));
+  }
+  ctx->last_rounds = rounds;
   return FRG_OK;
 }
 
@@ -342,7 +390,7 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
   FRG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   for (Out& o : outs)
     if (o.user && o.host) FRG_CUDA(ctx, cudaMemcpyAsync(o.user, o.dev, o.bytes, cudaMemcpyDeviceToHost, st));
-  unsigned long long cnt[24], qv[4];
+  unsigned long long cnt[40], qv[4];
   FRG_CUDA(ctx, cudaMemcpyAsync(cnt, ctx->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
   FRG_CUDA(ctx, cudaMemcpyAsync(qv, ctx->queue.p, sizeof(qv), cudaMemcpyDeviceToHost, st));
   FRG_CUDA(ctx, cudaStreamSynchronize(st));
@@ -354,16 +402,20 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
     stats->fp64_solves = (int64_t)cnt[11];
     stats->handoffs = (int64_t)cnt[12];
     for (int r = 0; r < 6; ++r) stats->handoff_reason[r] = (int64_t)cnt[16 + r];
+    for (int r = 0; r < 12; ++r) stats->kernel_cycles[r] = (int64_t)cnt[24 + r];
     (void)qv;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->track_ms = ms;
     if (ctx->cfg.precision == FRG_PREC_MIXED) {
-      float m0 = 0.f, m1 = 0.f;
-      cudaEventElapsedTime(&m0, ctx->ev0, ctx->evmid);
-      cudaEventElapsedTime(&m1, ctx->evmid, ctx->ev1);
-      stats->stage_ms[0] = m0;
-      stats->stage_ms[1] = m1;
+      for (int r = 0; r < ctx->last_rounds; ++r) {
+        float m0 = 0.f, m1 = 0.f;
+        cudaEventElapsedTime(&m0, ctx->round_ev[2 * r], ctx->round_ev[2 * r + 1]);
+        cudaEventElapsedTime(&m1, ctx->round_ev[2 * r + 1], ctx->round_ev[2 * r + 2]);
+        stats->stage_ms[0] += m0;
+        stats->stage_ms[1] += m1;
+      }
+      stats->handbacks = (int64_t)cnt[13];
     } else {
       stats->stage_ms[1] = ms;
     }

@@ -6,12 +6,16 @@
 
 #include "../../include/frg_gb300.h"
 #include "frg_complex.cuh"
+#include "frg_df.cuh"
 
 #ifndef FRG_TRACK_THREADS
 #define FRG_TRACK_THREADS 64
 #endif
 #ifndef FRG_TEAM_THREADS
 #define FRG_TEAM_THREADS 64
+#endif
+#ifndef FRG_MIXED_ROUNDS
+#define FRG_MIXED_ROUNDS 8  // FP32/FP64 rounds of a mixed-precision call
 #endif
 
 namespace frg {
@@ -23,6 +27,7 @@ struct Handoff {
   double s;
   uint64_t rng_index;
   int streak, step, ministep, tstepQ, n_ivp, n_newton, reason, code;  // reason 6: finished with code
+  int bounces, pad;  // times the path returned from FP64 to FP32
 };
 
 // Device-side arguments of one tracking launch. All arrays are device memory.
@@ -32,6 +37,8 @@ struct TrackArgs {
   const cx<double>* gamma;      // ntasks
   const cx<float>* fpm_lo;      // FP32 copies for the FP32 stage
   const cx<float>* gamma_lo;
+  const cx<df>* fpm_df;         // double-float copies for the FP32 stage's refinement residuals
+  const cx<df>* gamma_df;
   const int64_t* task_start;    // ntasks + 1 prefix sums of paths per task
   int ntasks;
   int64_t npaths;
@@ -45,8 +52,12 @@ struct TrackArgs {
   unsigned long long* counters; // 24: codes[8], ivp, newton, steps, fp64 solves, handoffs, -, -,
                                 //     handoff reasons 1..6 at [16..21]
   Handoff* handoff;             // npaths slots (mixed precision)
-  int64_t* handoff_list;        // ids of handed-off paths
+  int64_t* handoff_list;        // ids of paths handed to the FP64 kernel
   unsigned long long* handoff_count;
+  const int64_t* lo_list;       // FP32 kernel: paths to resume from their saved state (null: fresh paths)
+  const unsigned long long* lo_count;
+  int64_t* back_list;           // FP64 kernel: paths handed back to FP32 (null: none, e.g. the last round)
+  unsigned long long* back_count;
 };
 
 }  // namespace frg
@@ -57,3 +68,4 @@ cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_team(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
 cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);
+cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream);

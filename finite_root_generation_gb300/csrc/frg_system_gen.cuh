@@ -213,3 +213,54 @@ __device__ __forceinline__ void frg_group_eval(
   o.dIII[15] = (-x85) + x71*x73 - x87*x90 - P0*x132*x136 - Pc0*x133*x137 - x11*x134*x90 - x135*x16*x87 + P0*x132*x84*z + Pc0*x133*x79*z + Pcj*U*x134*x79 + (T(2.0)*(iU*x84*x90*z)) + Pj*iU*x135*x84*z2;
   o.tIII = dQcj*x110*(x20 + x20*x83) + dQj*x93*(x25 + x25*x78) + dP0*x132*z*((-x136) + x84*z) + dPc0*x133*z*((-x137) + x79*z) - dPcj*z*(x122 - x129)*(ec1*x113 + ec2*x82) - dPj*z*(x106 - x102)*(x116 - x111);
 }
+
+// The three equations alone: 62 complex mul, 57 complex add/sub, 0 real x complex.
+#define FRG_GENF_CMUL 62
+#define FRG_GENF_CADD 57
+template <typename T>
+__device__ __forceinline__ void frg_group_f(
+    const cx<T> A, const cx<T> B, const cx<T> C, const cx<T> D, const cx<T> F, const cx<T> G,
+    const cx<T> H, const cx<T> Ac, const cx<T> Bc, const cx<T> Cc, const cx<T> Dc, const cx<T> Fc,
+    const cx<T> Gc, const cx<T> Hc, const cx<T> z,
+    const cx<T> e1, const cx<T> e2, const cx<T> ec1, const cx<T> ec2,
+    const cx<T> z2, const cx<T> z3, const cx<T> P0, const cx<T> Pc0,
+    const cx<T> U, const cx<T> iU, const cx<T> Pj, const cx<T> Pcj, const cx<T> Qj, const cx<T> Qcj,
+    cx<T>& fI, cx<T>& fII, cx<T>& fIII) {
+  const cx<T> y0 = z3*(P0*Pc0 + Pcj*Pj);
+  const cx<T> y1 = (-(Pc0*z));
+  const cx<T> y2 = (-(P0*z));
+  const cx<T> y3 = (-(Ac));
+  const cx<T> y4 = Pcj*z;
+  const cx<T> y5 = y3 + y4;
+  const cx<T> y6 = (-(A));
+  const cx<T> y7 = Pj*z;
+  const cx<T> y8 = y6 + y7;
+  const cx<T> y9 = (-(y7));
+  const cx<T> y10 = A + y9;
+  const cx<T> y11 = Ac - Cc;
+  const cx<T> y12 = Qcj*y11;
+  const cx<T> y13 = (-(y4));
+  const cx<T> y14 = Ac + y13;
+  const cx<T> y15 = A - C;
+  const cx<T> y16 = Qj*y15;
+  const cx<T> y17 = H + y2;
+  const cx<T> y18 = Hc + y1;
+  const cx<T> y19 = iU*z2;
+  const cx<T> y20 = Bc + y13;
+  const cx<T> y21 = F + y2;
+  const cx<T> y22 = B + y9;
+  const cx<T> y23 = Fc + y1;
+  const cx<T> y24 = (-(G));
+  const cx<T> y25 = (-(Gc));
+  const cx<T> y26 = e1*(B - D);
+  const cx<T> y27 = e2*(C + y24);
+  const cx<T> y28 = y21*y26 - y17*y27;
+  const cx<T> y29 = ec1*(Bc - Dc);
+  const cx<T> y30 = ec2*(Cc + y25);
+  const cx<T> y31 = y23*y29 - y18*y30;
+  const cx<T> y32 = Bc + y12 + y3 + y20*y29 - y30*(y14 - Qcj*y11);
+  const cx<T> y33 = B + y16 + y6 + y22*y26 - y27*(y10 - Qj*y15);
+  fI = (-y0) + A*z*(Cc + y5) + Ac*z*(C + y8) + U*y17*((-y12) - y5) + y10*y12*z + y14*y16*z + y18*y19*((-y16) - y8) - H*z*(Cc + y1) - Hc*z*(C + y2);
+  fII = (-y0) + z2*(B*Pcj + Bc*Pj) + U*y20*y21 - F*z*(Bc + y1) - Fc*z*(B + y2) + iU*y22*y23*z2;
+  fIII = U*y28*y32 + y19*y31*y33 + z*(D + y24)*(Dc + y25) - y28*y31*z - y32*y33*z;
+}

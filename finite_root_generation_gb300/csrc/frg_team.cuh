@@ -24,9 +24,15 @@
 #pragma once
 
 #include "frg_device.cuh"
+#include "frg_df.cuh"
 
 namespace frg {
 namespace team {
+
+// Type of the path's points (Yc, Yn, YN) and of the refinement residual: FP64 in the
+// FP64 kernels, double-float in the FP32 stage.
+template <typename T> struct PointOf { typedef double type; };
+template <> struct PointOf<float> { typedef df type; };
 
 constexpr int TEAM = 8;
 constexpr int NG = 16;  // links (14), Z0, t
@@ -46,6 +52,9 @@ __device__ __forceinline__ cx<T> shfl(unsigned mask, cx<T> v, int src) {
 template <typename T>
 __device__ __forceinline__ cx<T> shfl_xor(unsigned mask, cx<T> v, int off) {
   return cx<T>(__shfl_xor_sync(mask, v.re, off, TEAM), __shfl_xor_sync(mask, v.im, off, TEAM));
+}
+__device__ __forceinline__ df shfl_xor(unsigned mask, df v, int off) {
+  return df(__shfl_xor_sync(mask, v.hi, off, TEAM), __shfl_xor_sync(mask, v.lo, off, TEAM));
 }
 template <typename T>
 __device__ __forceinline__ T team_sum(unsigned mask, T v) {
@@ -69,13 +78,22 @@ __device__ __forceinline__ T team_min(unsigned mask, T v) {
   return v;
 }
 
-// Per-team shared state of one path, in the working precision. The 32-byte pad
-// makes the stride between teams 32 bytes past a multiple of 128, so the four teams
-// of a warp reading "the same" field hit four different bank groups.
+// Per-team shared state of one path. The points Yc (accepted), Yn (predicted) and
+// YN (corrector iterate) are FP64 in every mode, so corrector iterations of the FP32
+// stage refine in FP64 (FP64 residual, FP32 solve); directions, patches and
+// stage vectors are in the working precision T. U/Urhs hold the reduced system's
+// upper factor for the back substitution. The 32-byte pad makes the stride between
+// teams 32 bytes past a multiple of 128, so the four teams of a warp reading "the
+// same" field hit different bank groups.
 template <typename T>
 struct Smem {
-  cx<T> Yc[VS], Vc[VS], Yn[VS], Vn[VS], YN[VS], u[VS], Ye[VS], dx[VS];
+  typedef typename PointOf<T>::type P;
+  cx<P> Yc[VS], Yn[VS], YN[VS];
+  cx<P> spm[32];
+  cx<T> Vc[VS], Vn[VS], u[VS], Ye[VS], dx[VS];
   cx<T> k[8][VS];
+  cx<T> U[16][16];
+  cx<T> Urhs[16];
   unsigned char pad[32];
 };
 
@@ -104,20 +122,109 @@ struct StepOut {
   T hnorm;   // |H| at the evaluation point (Newton)
 };
 
+// The team's residual F_j (its three equations) at the point Yd with q(t), all in
+// the point type P (htpysupport.cu:37-48, :64-86): the FP32 stage's corrector uses it
+// as the right-hand side, so its iterates converge in double-float although J and
+// the LU are FP32.
+template <typename P>
+__device__ __forceinline__ void residual_hi(const cx<P>* Yd, const cx<P>* spm, const cx<P>* fpm, cx<P> gamma,
+                                            int j, cx<P>& fI, cx<P>& fII, cx<P>& fIII) {
+  typedef cx<P> cp;
+  const P t = Yd[22].re;
+  const cp g1t = gamma * (P(1) - t);
+  const cp iden = cinv(g1t + cp(t));
+  cp q[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const int pi = param_index(i, j);
+    q[i] = (g1t * spm[pi] + t * fpm[pi]) * iden;
+  }
+  const cp z = Yd[21], z2 = z * z, z3 = z2 * z, U = Yd[13 + j];
+  frg_group_f<P>(Yd[0], Yd[1], Yd[2], Yd[3], Yd[4], Yd[5], Yd[6], Yd[7], Yd[8], Yd[9], Yd[10], Yd[11],
+                      Yd[12], Yd[13], z, cinv(Yd[4] - Yd[1]), cinv(Yd[6] - Yd[2]), cinv(Yd[11] - Yd[8]),
+                      cinv(Yd[13] - Yd[9]), z2, z3, q[0], q[1], U, cinv(U), q[2], q[3], q[4], q[5], fI, fII, fIII);
+}
+
+// One step of the dense phase over a window of W columns: the current pivot column
+// is index 0; rows shift one column left as they are eliminated, so a rolled loop
+// needs no dynamic register indexing. The pivot row (final once chosen) goes to S.U.
+template <typename T, int W>
+__device__ __forceinline__ void lu_window_step(Smem<T>& S, int k, int g, cx<T>* R0, cx<T>& R0r, cx<T>* R1,
+                                               cx<T>& R1r, bool& used0, bool& used1, T& pmax, T& pmin) {
+  const unsigned FULL = 0xffffffffu;
+  const cx<T> zero(T(0));
+  const T v0 = used0 ? T(-1) : cnorm2(R0[0]);
+  const T v1 = used1 ? T(-1) : cnorm2(R1[0]);
+  T bv = v0 >= v1 ? v0 : v1;
+  int bk = 2 * g + (v0 >= v1 ? 0 : 1);
+#pragma unroll
+  for (int off = 4; off >= 1; off >>= 1) {
+    const T ov = shfl_xor(FULL, bv, off);
+    const int ok = shfl_xor(FULL, bk, off);
+    if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; }
+  }
+  const int pl = bk >> 1, ps = bk & 1;
+  if (g == pl) { if (ps) used1 = true; else used0 = true; }
+  cx<T> prow[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) prow[c] = shfl(FULL, ps ? R1[c] : R0[c], pl);
+  const cx<T> prhs = shfl(FULL, ps ? R1r : R0r, pl);
+  if (g == 0) {
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      if (k + c < 16) S.U[k][k + c] = prow[c];
+    S.Urhs[k] = prhs;
+  }
+  const cx<T> ip = cinv(prow[0]);
+  const T pa = sqrt(cnorm2(prow[0]));
+  pmax = fmax(pmax, pa);
+  pmin = fmin(pmin, pa);
+  const cx<T> l0 = used0 ? zero : R0[0] * ip;
+  const cx<T> l1 = used1 ? zero : R1[0] * ip;
+#pragma unroll
+  for (int c = 0; c + 1 < W; ++c) {
+    R0[c] = cfms(R0[c + 1], l0, prow[c + 1]);
+    R1[c] = cfms(R1[c + 1], l1, prow[c + 1]);
+  }
+  R0[W - 1] = zero;
+  R1[W - 1] = zero;
+  R0r = cfms(R0r, l0, prhs);
+  R1r = cfms(R1r, l1, prhs);
+}
+
 // One linear-system step, executed convergently by the whole warp (full-mask
 // shuffles inside). Each team evaluates at its S.Ye:
 //   tangent (newton = false): [JH; W] x = e_23 with W = the velocity patch Wsrc,
 //     then normalised to unit length with real dt/ds (or dt = 1 when tstep),
 //     Im(dt) = 0 (htpysupport.cu:237-299);
-//   Newton (newton = true): [JH; e_t] x = [-H; tgoal - t] (htpysupport.cu:427-477).
+//   Newton (newton = true): [JH; e_t] x = [-H; tgoal - t] (htpysupport.cu:427-477),
+//     H at the FP64 point S.YN; when T is float, H is evaluated in FP64 if `hires`
+//     and in FP32 (at the rounded point) otherwise.
 // The solution is written to dst[0..22] (shared memory).
 template <typename T>
 __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc, cx<T>* dst, bool newton,
-                                                  bool tstep, T tgoal, const LaneParams<T>& lp, int g) {
+                                                  bool tstep, T tgoal, const LaneParams<T>& lp,
+                                                  const cx<typename PointOf<T>::type>* fpm_hi,
+                                                  cx<typename PointOf<T>::type> gamma_hi, int g, bool hires) {
+  typedef typename PointOf<T>::type P;
   const unsigned FULL = 0xffffffffu;
   const bool grp = g < 7;
   const int j = grp ? g + 1 : 7;
   const cx<T> zero(T(0));
+  constexpr bool LOWP = sizeof(T) < sizeof(double);
+
+  // ---- FP64 residual of the corrector (FP32 stage only)
+  cx<T> hF0 = zero, hF1 = zero, hF2 = zero, hU = zero;
+  T hsq = T(0);
+  if (LOWP && newton && hires) {
+    cx<P> fI, fII, fIII;
+    residual_hi<P>(S.YN, S.spm, fpm_hi, gamma_hi, j, fI, fII, fIII);
+    cx<P> d(P(0));
+    for (int e = 0; e < 23; ++e) d = cfma(cx<P>(S.u[e]), S.YN[e], d);
+    d = d - cx<P>(P(1));
+    hF0 = cx<T>(fI); hF1 = cx<T>(fII); hF2 = cx<T>(fIII); hU = cx<T>(d);
+    hsq = grp ? T(cnorm2(hF0) + cnorm2(hF1) + cnorm2(hF2)) : T(cnorm2(hU));
+  }
 
   // ---- evaluation point and parameters q(t), dq/dt (htpysupport.cu:37-62)
   const cx<T> A = S.Ye[0], B = S.Ye[1], C = S.Ye[2], D = S.Ye[3], F = S.Ye[4], G = S.Ye[5], H = S.Ye[6];
@@ -145,6 +252,11 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
                       cinv(Fc - Bc), cinv(Hc - Cc), z2, z3, q[0], q[1], dq[0], dq[1], U, cinv(U), q[2], q[3],
                       q[4], q[5], dq[2], dq[3], dq[4], dq[5], o);
   }
+  const bool lores_h = !LOWP || !hires;  // H from the working-precision evaluation
+  if (lores_h) {
+    hF0 = o.fI; hF1 = o.fII; hF2 = o.fIII;
+    hsq = grp ? cnorm2(o.fI) + cnorm2(o.fII) + cnorm2(o.fIII) : T(0);
+  }
   // rows in local column order: 0..13 links, 14 Z0, 15 t, 16 U_j, 17 rhs
   cx<T> r0[18], r1[18], r2[18];
 #pragma unroll
@@ -156,8 +268,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
 #pragma unroll
   for (int c = 0; c < 14; ++c) r2[c] = o.dIII[c];
   r2[16] = o.dIII[14]; r2[14] = o.dIII[15]; r2[15] = o.tIII;
-  if (newton) { r0[17] = -o.fI; r1[17] = -o.fII; r2[17] = -o.fIII; }
-  T hsq = grp ? cnorm2(o.fI) + cnorm2(o.fII) + cnorm2(o.fIII) : T(0);
+  if (newton) { r0[17] = -hF0; r1[17] = -hF1; r2[17] = -hF2; }
   // row scaling by 1/max(|re|,|im|) (htpysupport.cu:259-277, :446-471)
   {
     T m0 = T(0), m1 = T(0), m2 = T(0);
@@ -174,7 +285,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   // ---- eliminate U_j inside the group: partial pivoting among its three rows
   const T a0 = cnorm2(r0[16]), a1 = cnorm2(r1[16]), a2 = cnorm2(r2[16]);
   const int p = (a0 >= a1 && a0 >= a2) ? 0 : (a1 >= a2 ? 1 : 2);
-  cx<T> piv[18], ra[17], rb[17];
+  cx<T> piv[18], R0[16], R1[16], R0r, R1r;
 #pragma unroll
   for (int c = 0; c < 18; ++c) piv[c] = p == 0 ? r0[c] : (p == 1 ? r1[c] : r2[c]);
   cx<T> ipu = cinv(piv[16]);
@@ -186,8 +297,9 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
       const int cc = c < 16 ? c : 17;
       const cx<T> xa = p == 0 ? r1[cc] : r0[cc];
       const cx<T> xb = p == 2 ? r1[cc] : r2[cc];
-      ra[c] = cfms(xa, la, piv[cc]);
-      rb[c] = cfms(xb, lb, piv[cc]);
+      const cx<T> ya = cfms(xa, la, piv[cc]);
+      const cx<T> yb = cfms(xb, lb, piv[cc]);
+      if (c < 16) { R0[c] = ya; R1[c] = yb; } else { R0r = ya; R1r = yb; }
     }
   }
   // ---- patch rows (lane 7) and the folding of every group's pivot row into them
@@ -197,13 +309,16 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   for (int e = 0; e < 23; ++e) su = fmax(su, fmax(tabs(u[e].re), tabs(u[e].im)));
   su = T(1) / su;
   const T tdiff = tgoal - t;
-  cx<T> hu(T(0));
-  if (newton) {
+  if (lores_h && newton) {
+    cx<T> d(T(0));
 #pragma unroll
-    for (int e = 0; e < 23; ++e) hu = cfma(u[e], S.Ye[e], hu);
-    hu = hu - cx<T>(T(1));
+    for (int e = 0; e < 23; ++e) d = cfma(u[e], S.Ye[e], d);
+    hU = d - cx<T>(T(1));
   }
-  if (!grp) { hsq = cnorm2(hu); ipu = zero; }
+  if (!grp) {
+    if (lores_h) hsq = cnorm2(hU);
+    ipu = zero;
+  }
   const cx<T> mu = (su * u[13 + j]) * ipu;
   const cx<T> mw = newton ? zero : Wsrc[13 + j] * ipu;
   cx<T> Su[17], Sw[17];
@@ -221,72 +336,54 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
       Sw[c] += shfl_xor(FULL, Sw[c], off);
     }
   }
-  cx<T> R0[17], R1[17];
+  if (!grp) {
 #pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    const cx<T> uc = su * u[gstate(c)];
-    const cx<T> wc = newton ? (c == 15 ? cx<T>(T(1)) : zero) : Wsrc[gstate(c)];
-    R0[c] = grp ? ra[c] : uc - Su[c];
-    R1[c] = grp ? rb[c] : wc - Sw[c];
+    for (int c = 0; c < 16; ++c) {
+      R0[c] = su * u[gstate(c)] - Su[c];
+      R1[c] = (newton ? (c == 15 ? cx<T>(T(1)) : zero) : Wsrc[gstate(c)]) - Sw[c];
+    }
+    R0r = (newton ? -(su * hU) : zero) - Su[16];
+    R1r = (newton ? cx<T>(tdiff) : cx<T>(T(1))) - Sw[16];
   }
-  R0[16] = grp ? ra[16] : (newton ? -(su * hu) : zero) - Su[16];
-  R1[16] = grp ? rb[16] : (newton ? cx<T>(tdiff) : cx<T>(T(1))) - Sw[16];
 
-  // ---- dense 16 x 16 LU with partial pivoting across the team
-  int step0 = 99, step1 = 99;  // elimination step at which each row became a pivot
-  cx<T> ipiv[16];
-  int powner[16];
+  // ---- dense 16 x 16 LU with partial pivoting across the team: 8 steps over a
+  //      16-wide window, then 8 over the remaining 8 columns
+  bool used0 = false, used1 = false;
   T pmax = T(0), pmin = T(3.0e38);
+#pragma unroll 1
+  for (int k = 0; k < 8; ++k) lu_window_step<T, 16>(S, k, g, R0, R0r, R1, R1r, used0, used1, pmax, pmin);
+  {
+    cx<T> Q0[8], Q1[8];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const T v0 = step0 < 99 ? T(-1) : cnorm2(R0[k]);
-    const T v1 = step1 < 99 ? T(-1) : cnorm2(R1[k]);
-    T bv = v0 >= v1 ? v0 : v1;
-    int bk = 2 * g + (v0 >= v1 ? 0 : 1);
-#pragma unroll
-    for (int off = 4; off >= 1; off >>= 1) {
-      const T ov = shfl_xor(FULL, bv, off);
-      const int ok = shfl_xor(FULL, bk, off);
-      if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; }
-    }
-    const int pl = bk >> 1, ps = bk & 1;
-    powner[k] = bk;
-    if (g == pl) { if (ps) step1 = k; else step0 = k; }
-    cx<T> prow[17];
-#pragma unroll
-    for (int c = k; c < 17; ++c) prow[c] = shfl(FULL, ps ? R1[c] : R0[c], pl);
-    const cx<T> ip = cinv(prow[k]);
-    ipiv[k] = ip;
-    const T pa = sqrt(cnorm2(prow[k]));
-    pmax = fmax(pmax, pa);
-    pmin = fmin(pmin, pa);
-    const cx<T> l0 = step0 < 99 ? zero : R0[k] * ip;
-    const cx<T> l1 = step1 < 99 ? zero : R1[k] * ip;
-#pragma unroll
-    for (int c = k + 1; c < 17; ++c) {
-      R0[c] = cfms(R0[c], l0, prow[c]);
-      R1[c] = cfms(R1[c], l1, prow[c]);
-    }
+    for (int c = 0; c < 8; ++c) { Q0[c] = R0[c]; Q1[c] = R1[c]; }
+#pragma unroll 1
+    for (int k = 8; k < 16; ++k) lu_window_step<T, 8>(S, k, g, Q0, R0r, Q1, R1r, used0, used1, pmax, pmin);
   }
-  // ---- back substitution, column by column
+  __syncwarp();
+  // ---- back substitution, column by column; lane g keeps the right-hand sides of
+  //      pivot rows g and g + 8
+  cx<T> rb0 = S.Urhs[g], rb1 = S.Urhs[g + 8];
+  __syncwarp();
+#pragma unroll 1
+  for (int k = 15; k >= 0; --k) {
+    const cx<T> mine = ((k >> 3) ? rb1 : rb0) * cinv(S.U[k][k]);
+    const cx<T> xk = shfl(FULL, mine, k & 7);
+    if (g == 0) S.Urhs[k] = xk;
+    if (g < k) rb0 = cfms(rb0, S.U[g][k], xk);
+    if (g + 8 < k) rb1 = cfms(rb1, S.U[g + 8][k], xk);
+  }
+  __syncwarp();
   cx<T> xg[16];
 #pragma unroll
-  for (int k = 15; k >= 0; --k) {
-    const int pl = powner[k] >> 1, ps = powner[k] & 1;
-    const cx<T> mine = (ps ? R1[16] : R0[16]) * ipiv[k];
-    const cx<T> xk = shfl(FULL, mine, pl);
-    xg[k] = xk;
-    const cx<T> m0 = step0 < k ? R0[k] : zero;
-    const cx<T> m1 = step1 < k ? R1[k] : zero;
-    R0[16] = cfms(R0[16], m0, xk);
-    R1[16] = cfms(R1[16], m1, xk);
-  }
+  for (int c = 0; c < 16; ++c) xg[c] = S.Urhs[c];
   // ---- U_j from the group's pivot row
   cx<T> xu = piv[17];
 #pragma unroll
   for (int c = 0; c < 16; ++c) xu = cfms(xu, piv[c], xg[c]);
   xu = xu * ipu;
-  // ---- pivot ratio over all 23 pivots
+  // ---- condition estimate: the pivot ratio over all 23 pivots. A small group pivot
+  //      (a U_j column weak in its group's rows, where a dense elimination would pivot
+  //      on a patch row) makes this elimination lose accuracy, so it counts too.
   {
     const T gp = grp ? sqrt(cnorm2(piv[16])) : pmax;
     pmax = fmax(pmax, team_max(FULL, gp));
@@ -312,6 +409,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
     n2 = n2 * cnorm2(sc);
   }
   out.xnorm2 = n2;
+  __syncwarp();
   if (grp) dst[13 + j] = xu;
 #pragma unroll
   for (int c = 0; c < 16; ++c)

@@ -450,6 +450,10 @@ __global__ void to_float_kernel(const cx<double>* in, cx<float>* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = cx<float>(in[i]);
 }
+__global__ void to_df_kernel(const cx<double>* in, cx<df>* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cx<df>(df(in[i].re), df(in[i].im));
+}
 
 template <int MODE, typename T>
 cudaError_t launch(const frg::TrackArgs& args, int grid, cudaStream_t stream) {
@@ -470,6 +474,12 @@ cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cud
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   to_float_kernel<<<(n + 127) / 128, 128, 0, stream>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  to_df_kernel<<<(n + 127) / 128, 128, 0, stream>>>(in, out, n);
   return cudaGetLastError();
 }
 

@@ -85,6 +85,21 @@ template <> __device__ __forceinline__ const cx<double>* fpm_of<double>(const Tr
 template <> __device__ __forceinline__ const cx<float>* fpm_of<float>(const TrackArgs& a, int task) {
   return a.fpm_lo + (size_t)task * NP;
 }
+// the task's parameters and gamma in the point type (FP64, or double-float)
+template <typename P> __device__ __forceinline__ const cx<P>* fpm_hi_of(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ const cx<double>* fpm_hi_of<double>(const TrackArgs& a, int task) {
+  return a.fpm + (size_t)task * NP;
+}
+template <> __device__ __forceinline__ const cx<df>* fpm_hi_of<df>(const TrackArgs& a, int task) {
+  return a.fpm_df + (size_t)task * NP;
+}
+template <typename P> __device__ __forceinline__ cx<P> gamma_hi_of(const TrackArgs& a, int task);
+template <> __device__ __forceinline__ cx<double> gamma_hi_of<double>(const TrackArgs& a, int task) {
+  return a.gamma[task];
+}
+template <> __device__ __forceinline__ cx<df> gamma_hi_of<df>(const TrackArgs& a, int task) {
+  return a.gamma_df[task];
+}
 template <typename T> __device__ __forceinline__ cx<T> gamma_of(const TrackArgs& a, int task);
 template <> __device__ __forceinline__ cx<double> gamma_of<double>(const TrackArgs& a, int task) {
   return a.gamma[task];
@@ -177,14 +192,27 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   const int lane = threadIdx.x & 31;
   const int g = lane & 7;
   const unsigned tmask = 0xffu << (lane & 24);
+  typedef typename PointOf<T>::type P;
+  typedef cx<P> cp;
   Smem<T>& S = reinterpret_cast<Smem<T>*>(smem_raw)[threadIdx.x >> 3];
   {
     cx<T>* base = reinterpret_cast<cx<T>*>(&S);
     for (int i = g; i < (int)(sizeof(Smem<T>) / sizeof(cx<T>)); i += TEAM) base[i] = cx<T>(T(0));
   }
-  const T newt_tol = LO ? T(c.newt_tol_lo) : T(c.newt_tol);
+  // The FP32 stage's corrector iterates on FP32 residuals until |dY| falls below
+  // newt_tol_lo (or stops shrinking), then on FP64 residuals to the reference's
+  // newt_tol: an FP32 LU with FP64 residuals converges like FP64 Newton while the
+  // pivot ratio stays below cond_switch.
+  const T newt_tol = T(c.newt_tol);
   const int jg = g < 7 ? g + 1 : 7;
-  const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count : a.npaths;
+  // what this launch works through: fresh paths, paths resumed in FP32 (lo_list),
+  // or paths handed to FP64 (handoff_list)
+  const bool lo_resume = LO && a.lo_list != nullptr;
+  const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count
+                         : (lo_resume ? (int64_t)*a.lo_count : a.npaths);
+  // a path returns from FP64 to FP32 after this many consecutive well-conditioned solves
+  constexpr int kBackSteps = 16;
+  constexpr int kMaxBounces = 8;
 
   LaneParams<T> lp;
   int64_t id = -1;
@@ -194,17 +222,25 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   int n_ivp = 0, n_newton = 0;
   uint64_t rng_index = 0;
   int phase = PH_FETCH;
+  bool hires = !LO;
+  T res_prev = T(0);
+  int good = 0, bounces = 0;
   unsigned long long fp64_solves = 0;
+  // cycle accounting (lane 0 of each warp): fetch, setup, linear step, transitions;
+  // warp steps and active-team steps
+  long long cyc[4] = {0, 0, 0, 0};
+  long long warp_steps = 0, team_steps = 0;
   __syncwarp();
 
   for (;;) {
+    long long tc0 = clock64();
     // =========================================================== fetch (per team)
     while (phase == PH_FETCH) {
       unsigned long long qi = 0;
       if (g == 0) qi = atomicAdd(a.queue, 1ull);
       qi = __shfl_sync(tmask, qi, 0, TEAM);
       if ((int64_t)qi >= nqueue) { phase = PH_IDLE; break; }
-      id = (MODE == MODE_RESUME) ? a.handoff_list[qi] : (int64_t)qi;
+      id = (MODE == MODE_RESUME) ? a.handoff_list[qi] : (lo_resume ? a.lo_list[qi] : (int64_t)qi);
       int lo = 0, hi = a.ntasks - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -218,20 +254,25 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
 #pragma unroll
         for (int i = 0; i < 6; ++i) { lp.sp[i] = cx<T>(sp[i]); lp.fp[i] = fpmT[param_index(i, jg)]; }
         lp.gamma = gamma_of<T>(a, task);
-        if (MODE != MODE_RESUME) {
-          for (int e = g; e < 14; e += TEAM) S.Yc[e] = cx<T>(z[e]);
-          if (g < 7) S.Yc[13 + jg] = cx<T>(Uj);
-          if (g == 7) { S.Yc[21] = cx<T>(T(1)); S.Yc[22] = cx<T>(T(0)); }
+        if (g < 7) {
+          S.spm[jg] = cp(sp[2]); S.spm[8 + jg] = cp(sp[3]); S.spm[15 + jg] = cp(sp[4]); S.spm[22 + jg] = cp(sp[5]);
+        }
+        if (g == 0) { S.spm[0] = cp(sp[0]); S.spm[8] = cp(sp[1]); }
+        if (MODE != MODE_RESUME && !lo_resume) {
+          for (int e = g; e < 14; e += TEAM) S.Yc[e] = cp(z[e]);
+          if (g < 7) S.Yc[13 + jg] = cp(Uj);
+          if (g == 7) { S.Yc[21] = cp(P(1)); S.Yc[22] = cp(P(0)); }
         }
       }
       code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
-      if (MODE == MODE_RESUME) {
+      good = 0; bounces = 0;
+      if (MODE == MODE_RESUME || lo_resume) {
         const Handoff& h = a.handoff[id];
         for (int e = g; e < NY; e += TEAM) {
-          S.Yc[e] = cx<T>(h.Yc[e]); S.Vc[e] = cx<T>(h.Vc[e]); S.u[e] = cx<T>(h.u[e]);
+          S.Yc[e] = cp(h.Yc[e]); S.Vc[e] = cx<T>(h.Vc[e]); S.u[e] = cx<T>(h.u[e]);
         }
         s = T(h.s); rng_index = h.rng_index; streak = h.streak; step = h.step; ministep = h.ministep;
-        tstepQ = h.tstepQ; n_ivp = h.n_ivp; n_newton = h.n_newton;
+        tstepQ = h.tstepQ; n_ivp = h.n_ivp; n_newton = h.n_newton; bounces = h.bounces;
         __syncwarp(tmask);
         if (h.reason == 6) {  // the path already ended on a step limit in the FP32 stage
           if constexpr (!LO) {
@@ -256,11 +297,11 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         }
         rng_index = 92;
         __syncwarp(tmask);
-        // SwitchPatch(u, Yc, Yc) (htpytrack.cu:60)
-        cx<T> d(T(0));
-        for (int e = g; e < NZ; e += TEAM) d = cfma(S.u[e], S.Yc[e], d);
-        d = cx<T>(team_sum(tmask, d.re), team_sum(tmask, d.im));
-        const cx<T> sc = cdiv(cx<T>(T(1)) - S.u[22] * S.Yc[22], d);
+        // SwitchPatch(u, Yc, Yc) (htpytrack.cu:60), in the point type
+        cp d(P(0));
+        for (int e = g; e < NZ; e += TEAM) d = cfma(cp(S.u[e]), S.Yc[e], d);
+        d = cp(team_sum(tmask, d.re), team_sum(tmask, d.im));
+        const cp sc = cdiv(cp(P(1)) - cp(S.u[22]) * S.Yc[22], d);
         __syncwarp(tmask);
         for (int e = g; e < NZ; e += TEAM) S.Yc[e] = sc * S.Yc[e];
         s = T(c.s_init); tstepQ = 0; streak = c.caution_steps - 1; step = 0; ministep = 0;
@@ -269,6 +310,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       }
     }
     if (__all_sync(FULL, phase == PH_IDLE)) break;
+    long long tc1 = clock64();
 
     // ==================================================== set up (per team)
     const bool newton = (phase == PH_NEWTON || phase == PH_SHARP);
@@ -277,37 +319,50 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     const cx<T>* Wsrc = S.Vc;
     cx<T>* dst = S.dx;
     if (phase == PH_TANGENT0 || phase == PH_IDLE) {
-      for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.Yc[e];
+      for (int e = g; e < NY; e += TEAM) S.Ye[e] = cx<T>(S.Yc[e]);
     } else if (phase == PH_RK) {
       tstep = tstepQ != 0;
       dst = S.k[stage];
       if (stage == 0) {
-        for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.Yc[e];
+        for (int e = g; e < NY; e += TEAM) S.Ye[e] = cx<T>(S.Yc[e]);
       } else {
         Wsrc = S.k[stage - 1];
         const double* w = c_dpA[stage];
         for (int e = g; e < NY; e += TEAM) {
           cx<T> acc = T(w[stage - 1]) * s * S.k[stage - 1][e];
           for (int l = stage - 2; l >= 0; --l) acc = T(w[l]) * s * S.k[l][e] + acc;
-          S.Ye[e] = S.Yc[e] + acc;
+          S.Ye[e] = cx<T>(S.Yc[e]) + acc;
         }
       }
     } else {
-      tgoal = (phase == PH_SHARP) ? T(1) : S.Yn[22].re;
-      for (int e = g; e < NY; e += TEAM) S.Ye[e] = S.YN[e];
+      tgoal = (phase == PH_SHARP) ? T(1) : T(S.Yn[22].re);
+      for (int e = g; e < NY; e += TEAM) S.Ye[e] = cx<T>(S.YN[e]);
     }
     __syncwarp();
+    long long tc2 = clock64();
 
     // ========================================== linear step (whole warp)
-    const StepOut<T> r = linear_step<T>(S, Wsrc, dst, newton, tstep, tgoal, lp, g);
+    const StepOut<T> r = linear_step<T>(S, Wsrc, dst, newton, tstep, tgoal, lp, fpm_hi_of<P>(a, task),
+                                        gamma_hi_of<P>(a, task), g, hires);
     __syncwarp();
+    long long tc3 = clock64();
+    if (lane == 0) {
+      cyc[0] += tc1 - tc0; cyc[1] += tc2 - tc1; cyc[2] += tc3 - tc2;
+      warp_steps++;
+    }
+    {
+      const unsigned act = __ballot_sync(FULL, phase != PH_IDLE && g == 0);
+      if (lane == 0) team_steps += __popc(act);
+    }
     if (phase == PH_IDLE) continue;
     if (!LO) ++fp64_solves;
+    if (MODE == MODE_RESUME) good = (r.ratio < T(c.cond_switch * 1e-2)) ? good + 1 : 0;
     if (newton) ++n_newton; else ++n_ivp;
 
     // ============================================= transitions (per team)
     bool finished = false;
     int handoff = 0;
+    bool handback = false;
     bool final_from_YN = false;
     if (LO && !(r.ratio <= T(c.cond_switch))) {
       handoff = 2;  // ill-conditioned (or non-finite) step: continue in FP64 from Yc
@@ -329,7 +384,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
             if (c_dpB[l] != 0.0) yb = T(c_dpB[l]) * s * S.k[l][e] + yb;
           }
           es += cnorm2(le);
-          S.Yn[e] = S.Yc[e] + yb;
+          S.Yn[e] = S.Yc[e] + cp(yb);
           S.Vn[e] = S.k[7][e];
         }
         err = sqrt(team_sum(tmask, es));
@@ -338,15 +393,18 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         __syncwarp(tmask);
         if (ministep++ == c.max_ministeps) { code = 2; finished = true; }
         else if (err <= T(c.rk_tol)) {
-          const T tn = S.Yn[22].re;
-          if (LO && tn > T(1.0 - c.nudge_trigger)) handoff = 5;  // the endgame runs in FP64
-          else if (tn <= T(1.0 - c.nudge_trigger)) { attempt = 0; phase = PH_NEWTON; }
-          else if (fabs(T(1) - tn) < T(c.sharp_trigger)) { attempt = 0; phase = PH_SHARP; }
-          else { tstepQ = 1; s = T(1) - S.Yc[22].re; }  // land on t = 1 (htpytrack.cu:120-123)
+          const double tn = double(S.Yn[22].re);
+          if (LO && !c.lo_endgame && tn > 1.0 - c.nudge_trigger) handoff = 5;  // the endgame runs in FP64
+          else if (tn <= 1.0 - c.nudge_trigger) { attempt = 0; phase = PH_NEWTON; }
+          else if (fabs(1.0 - tn) < c.sharp_trigger) { attempt = 0; phase = PH_SHARP; }
+          else { tstepQ = 1; s = T(1.0 - double(S.Yc[22].re)); }  // land on t = 1 (htpytrack.cu:120-123)
           if (phase == PH_NEWTON || phase == PH_SHARP) {
             for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+            // the FP32 stage sharpens at exactly t = 1 (its t-update is only FP32-accurate)
+            if (LO && phase == PH_SHARP && g == (22 & 7)) S.YN[22] = cp(P(1));
             residual = T(100);
             it = 0;
+            hires = !LO || phase == PH_SHARP;
           }
         } else if (s <= T(c.s_min)) {
           if (LO) handoff = 4; else { code = 3; finished = true; }
@@ -361,29 +419,41 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       const bool sharp = (phase == PH_SHARP);
       const int max_its = sharp ? c.sharp_its : c.newt_its;
       const T tol = sharp ? T(c.sharp_tol) : newt_tol;
-      const int restype = sharp ? c.sharp_residual : c.newt_residual;
+      const int restype = (LO || sharp) ? (LO ? 1 : c.sharp_residual) : c.newt_residual;
       bool done = false;
       if (restype == 0 && it > 0) {
         residual = r.hnorm;  // |H| at the current point: the residual of the previous update
         if (!(it < max_its && residual > tol)) done = true;
       }
       if (!done) {
-        for (int e = g; e < NY; e += TEAM) S.YN[e] += S.dx[e];
+        for (int e = g; e < NY; e += TEAM) S.YN[e] += cp(S.dx[e]);
         it++;
         if (restype != 0) {
           residual = sqrt(r.xnorm2);
-          if (!(it < max_its && residual > tol)) done = true;
+          if (LO && !hires) {
+            // FP32 residuals: at the FP32 noise floor either accept (no refinement) or
+            // continue on double-float residuals to the reference's tolerance
+            const bool floor_ = residual < T(c.newt_tol_lo) || (it > 1 && residual > T(0.5) * res_prev);
+            if (floor_ && c.lo_refine) hires = true;
+            if ((floor_ && !c.lo_refine) || !(it < max_its)) done = true;
+          } else if (!(it < max_its && residual > tol)) {
+            done = true;
+          }
+          res_prev = residual;
         }
       }
       __syncwarp(tmask);
       if (done) {
-        const bool ok = residual < (sharp ? T(c.sharp_tol) : newt_tol);
+        const bool ok = (LO && !c.lo_refine && !sharp) ? residual < T(c.newt_tol_lo) * T(100)
+                                                        : (hires || !LO) && residual < (sharp ? T(c.sharp_tol) : newt_tol);
         if (ministep++ == c.max_ministeps) { code = 2; finished = true; final_from_YN = sharp; }
         else if (ok && !sharp) {
-          if (fabs(T(1) - S.Yn[22].re) < T(c.sharp_trigger)) {
+          if (fabs(1.0 - double(S.Yn[22].re)) < c.sharp_trigger) {
+            if (LO && !c.lo_endgame) handoff = 5;
             attempt = 0; phase = PH_SHARP;
             for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
-            residual = T(100); it = 0;
+            if (LO && g == (22 & 7)) S.YN[22] = cp(P(1));
+            residual = T(100); it = 0; hires = true;
           } else {
             // accept the step (htpytrack.cu:176-183)
             for (int e = g; e < NY; e += TEAM) { S.Yc[e] = S.YN[e]; S.Vc[e] = S.Vn[e]; }
@@ -394,7 +464,9 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
             else if (s < T(c.s_min)) s = T(c.s_min * 0.9);
             step++;
             if (step == c.max_steps) { code = 1; finished = true; }
-            else if (LO && S.YN[22].re >= T(c.t_switch)) handoff = 1;
+            else if (LO && !c.lo_endgame && double(S.YN[22].re) >= c.t_switch) handoff = 1;
+            else if (MODE == MODE_RESUME && a.back_list && good >= kBackSteps && bounces < kMaxBounces &&
+                     double(S.YN[22].re) < c.t_switch) handback = true;  // well conditioned again: back to FP32
             else { stage = 0; phase = PH_RK; }
           }
         } else if (ok && sharp) {
@@ -407,16 +479,16 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
                            T(2.0 * R * frg_uniform01(a.seed, id, rng_index + 2 * e + 1) - R));
           rng_index += 46;
           __syncwarp(tmask);
-          cx<T> d(T(0));
-          for (int e = g; e < NZ; e += TEAM) d = cfma(S.u[e], S.Yn[e], d);
-          d = cx<T>(team_sum(tmask, d.re), team_sum(tmask, d.im));
-          const cx<T> sc = cdiv(cx<T>(T(1)) - S.u[22] * S.Yn[22], d);
+          cp d(P(0));
+          for (int e = g; e < NZ; e += TEAM) d = cfma(cp(S.u[e]), S.Yn[e], d);
+          d = cp(team_sum(tmask, d.re), team_sum(tmask, d.im));
+          const cp sc = cdiv(cp(P(1)) - cp(S.u[22]) * S.Yn[22], d);
           __syncwarp(tmask);
           for (int e = g; e < NZ; e += TEAM) S.Yn[e] = sc * S.Yn[e];
           if (!sharp) {
             if (++attempt < c.newt_attempts) {
               for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
-              residual = T(100); it = 0;
+              residual = T(100); it = 0; hires = !LO;
             } else if (s <= T(c.s_min)) {
               if (LO) handoff = 3; else { code = 4; finished = true; }
             } else {
@@ -429,7 +501,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
           } else {
             if (++attempt < c.sharp_attempts) {
               for (int e = g; e < NY; e += TEAM) S.YN[e] = S.Yn[e];
+              if (LO && g == (22 & 7)) S.YN[22] = cp(P(1));
               residual = T(100); it = 0;
+            } else if (LO) {
+              handoff = 5;  // the FP32 stage could not sharpen: the FP64 kernel retries the endgame
             } else {
               code = 5; finished = true; final_from_YN = true;
             }
@@ -438,21 +513,30 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       }
     }
     __syncwarp(tmask);
+    if (lane == 0) cyc[3] += clock64() - tc3;
 
-    if (LO && (handoff || finished)) {
-      // save the state for the FP64 kernel (always: an FP32 path is finished in FP64)
+    if ((LO && (handoff || finished)) || handback) {
+      // save the state for the other precision's kernel (an FP32 path is always
+      // finished in FP64; an FP64 path well conditioned again returns to FP32)
       Handoff& h = a.handoff[id];
-      for (int e = g; e < NY; e += TEAM) { h.Yc[e] = cd(S.Yc[e]); h.Vc[e] = cd(S.Vc[e]); h.u[e] = cd(S.u[e]); }
+      const cp* ysrc = (finished && final_from_YN) ? S.YN : S.Yc;  // a sharpened root is in YN
+      for (int e = g; e < NY; e += TEAM) { h.Yc[e] = cd(ysrc[e]); h.Vc[e] = cd(S.Vc[e]); h.u[e] = cd(S.u[e]); }
       if (g == 0) {
         h.s = double(s); h.rng_index = rng_index; h.streak = streak; h.step = step; h.ministep = ministep;
         h.tstepQ = tstepQ; h.n_ivp = n_ivp; h.n_newton = n_newton;
         h.reason = finished ? 6 : handoff; h.code = code;
+        h.bounces = bounces + (handback ? 1 : 0);
         if (a.counters) {
-          if (!finished) atomicAdd(&a.counters[12], 1ull);
-          atomicAdd(&a.counters[15 + (finished ? 6 : handoff)], 1ull);
+          if (handback) atomicAdd(&a.counters[13], 1ull);
+          else {
+            if (!finished) atomicAdd(&a.counters[12], 1ull);
+            atomicAdd(&a.counters[15 + (finished ? 6 : handoff)], 1ull);
+          }
         }
-        const unsigned long long slot = atomicAdd(a.handoff_count, 1ull);
-        a.handoff_list[slot] = id;
+        unsigned long long* cnt = handback ? a.back_count : a.handoff_count;
+        int64_t* list = handback ? a.back_list : a.handoff_list;
+        const unsigned long long slot = atomicAdd(cnt, 1ull);
+        list[slot] = id;
       }
       __syncwarp(tmask);
       phase = PH_FETCH;
@@ -461,7 +545,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     if (finished) {
       if constexpr (!LO) {
         cd Yf[NY];
-        const cx<T>* src = final_from_YN ? S.YN : S.Yc;
+        const cp* src = final_from_YN ? S.YN : S.Yc;
         for (int e = 0; e < NY; ++e) Yf[e] = cd(src[e]);
         __syncwarp(tmask);
         team_finish(a, S, Yf, id, task, code, g, tmask, n_ivp, n_newton, step);
@@ -470,6 +554,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     }
   }
   if (a.counters && fp64_solves && g == 0) atomicAdd(&a.counters[11], fp64_solves);
+  if (a.counters && lane == 0) {
+    const int base = LO ? 24 : 30;
+    for (int i = 0; i < 4; ++i) atomicAdd(&a.counters[base + i], (unsigned long long)cyc[i]);
+    atomicAdd(&a.counters[base + 4], (unsigned long long)warp_steps);
+    atomicAdd(&a.counters[base + 5], (unsigned long long)team_steps);
+  }
 }
 
 }  // namespace team

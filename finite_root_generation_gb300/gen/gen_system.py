@@ -227,6 +227,30 @@ def main():
             lines.append(f"  o.d{fam}[{slot[fam]}] = {pr.expr(e)};")
             slot[fam] += 1
     lines.append("}")
+    # ---- F only (the three equations), for FP64 residuals next to FP32 Jacobians
+    f_outs = [fI, fII, fIII]
+    f_outs = [o.subs(z**3, shared_syms["z3"]).subs(z**2, shared_syms["z2"]) for o in f_outs]
+    frepl, fred = sp.cse(f_outs, symbols=sp.numbered_symbols("y"), optimizations="basic")
+    fcm, fca, fsm = count_ops([r for _, r in frepl] + fred)
+    lines.append("")
+    lines.append(f"// The three equations alone: {fcm} complex mul, {fca} complex add/sub, {fsm} real x complex.")
+    lines.append(f"#define FRG_GENF_CMUL {fcm}")
+    lines.append(f"#define FRG_GENF_CADD {fca}")
+    lines.append("template <typename T>")
+    lines.append("__device__ __forceinline__ void frg_group_f(")
+    lines.append("    const cx<T> A, const cx<T> B, const cx<T> C, const cx<T> D, const cx<T> F, const cx<T> G,")
+    lines.append("    const cx<T> H, const cx<T> Ac, const cx<T> Bc, const cx<T> Cc, const cx<T> Dc, const cx<T> Fc,")
+    lines.append("    const cx<T> Gc, const cx<T> Hc, const cx<T> z,")
+    lines.append("    const cx<T> e1, const cx<T> e2, const cx<T> ec1, const cx<T> ec2,")
+    lines.append("    const cx<T> z2, const cx<T> z3, const cx<T> P0, const cx<T> Pc0,")
+    lines.append("    const cx<T> U, const cx<T> iU, const cx<T> Pj, const cx<T> Pcj, const cx<T> Qj, const cx<T> Qcj,")
+    lines.append("    cx<T>& fI, cx<T>& fII, cx<T>& fIII) {")
+    for s_, e in frepl:
+        lines.append(f"  const cx<T> {s_} = {pr.expr(e)};")
+    lines.append(f"  fI = {pr.expr(fred[0])};")
+    lines.append(f"  fII = {pr.expr(fred[1])};")
+    lines.append(f"  fIII = {pr.expr(fred[2])};")
+    lines.append("}")
     used = set()
     for _, e in repl:
         used |= {s.name for s in e.free_symbols}
@@ -234,7 +258,8 @@ def main():
         used |= {s.name for s in e.free_symbols}
     with open(OUT, "w") as fh:
         fh.write("\n".join(lines) + "\n")
-    print(f"wrote {OUT}: {len(repl)} temporaries; per group {cm} cmul, {ca} cadd, {sm} smul")
+    print(f"wrote {OUT}: {len(repl)} temporaries; per group {cm} cmul, {ca} cadd, {sm} smul; "
+          f"F only {fcm} cmul, {fca} cadd")
     print("free inputs used:", sorted(u for u in used if not u.startswith("x")))
 
 

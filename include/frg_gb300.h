@@ -88,6 +88,12 @@ typedef struct frg_config {
   int blocks_per_sm;     /* 0 = tuned default */
   double newt_tol_lo;    /* mixed: corrector tolerance of the FP32 stage */
   int kernel_variant;    /* FRG_KERNEL_TEAM (8 lanes per path, default) or FRG_KERNEL_THREAD */
+  int mixed_rounds;      /* mixed, team kernels: FP32/FP64 rounds; a path well conditioned again in
+                            FP64 returns to FP32 in the next round (1 = no return) */
+  int lo_refine;         /* mixed: 1 = the FP32 corrector refines on double-float residuals to
+                            newt_tol; 0 = it stops at newt_tol_lo */
+  int lo_endgame;        /* mixed: 1 = the FP32 stage (with refinement) also runs the endgame and
+                            sharpening, FP64 only for ill-conditioned steps; 0 = FP64 from t_switch */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */
@@ -104,6 +110,10 @@ typedef struct frg_stats {
   double stage_ms[2];      /* device time of the FP32 stage and of the FP64 kernel */
   int64_t handoff_reason[6]; /* mixed: t_switch, ill-conditioned, corrector at s_min,
                                 predictor at s_min, endgame entry, ended on a step limit */
+  int64_t kernel_cycles[12]; /* team kernels, summed over warps: [0..5] FP32 stage, [6..11] FP64
+                                kernel; per kernel the cycles in path fetch, step set-up, linear steps
+                                and transitions, then warp steps and active-team steps */
+  int64_t handbacks;       /* mixed: returns from FP64 to FP32 once well conditioned again */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;

@@ -49,7 +49,10 @@ def test_mixed_residuals(runs):
 def test_mixed_uses_fp32_for_most_solves(runs):
     s = runs["mixed"].stats
     total = s["ivp_solves"] + s["newton_iters"]
-    assert 0 < s["handoffs"] <= s["paths"]
+    # a path may be handed to FP64 and back a bounded number of times (at most 8
+    # hand-backs), so hand-offs can exceed the path count but not 9x it
+    assert 0 < s["handoffs"] <= 9 * s["paths"]
+    assert s["handbacks"] <= 8 * s["paths"]
     assert s["fp64_solves"] < 0.5 * total
     assert runs["fp64"].stats["fp64_solves"] == runs["fp64"].stats["ivp_solves"] + runs["fp64"].stats["newton_iters"]
 

@@ -120,9 +120,10 @@ def test_oracle_config_knobs_match(tracker, oracle):
     res = t.track(REFERENCE_TARGET, [n], 3)
     ocfg = oracle.config(newt_residual=0, start_dist=1, start_range=1.0)
     r, c, _, _ = oracle.homotopy_batch(REFERENCE_TARGET, REFERENCE_GAMMA, 3, np.arange(n), cfg=ocfg)
-    assert (res.codes == c).mean() >= 0.97
-    ok = (c == 0) & (res.codes == 0)
-    assert (_rel(res.roots[ok], r[ok]) < ROOT_RTOL).mean() >= 0.97
+    ok = c == 0
+    same = (res.codes[ok] == 0) & (_rel(res.roots[ok], r[ok]) < ROOT_RTOL)
+    assert same.mean() >= 0.97
+    assert (res.codes == c).mean() >= 0.95
     t.close()
 
 
