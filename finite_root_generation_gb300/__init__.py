@@ -59,6 +59,7 @@ class FrgConfig(ctypes.Structure):
         ("threads_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
         ("newt_tol_lo", ctypes.c_double), ("kernel_variant", ctypes.c_int),
         ("mixed_rounds", ctypes.c_int), ("lo_refine", ctypes.c_int), ("lo_endgame", ctypes.c_int),
+        ("path_offset", ctypes.c_int64), ("fp64_budget", ctypes.c_int),
     ]
 
 
@@ -71,6 +72,7 @@ class FrgStats(ctypes.Structure):
         ("track_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("handoffs", ctypes.c_int64),
         ("stage_ms", ctypes.c_double * 2), ("handoff_reason", ctypes.c_int64 * 6),
         ("kernel_cycles", ctypes.c_int64 * 12), ("handbacks", ctypes.c_int64),
+        ("refine_solves", ctypes.c_int64), ("refine_warp_steps", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -78,7 +80,8 @@ class FrgStats(ctypes.Structure):
                 "newton_iters": self.newton_iters, "fp64_solves": self.fp64_solves, "steps": self.steps,
                 "track_ms": self.track_ms, "total_ms": self.total_ms, "handoffs": self.handoffs,
                 "stage_ms": list(self.stage_ms), "handoff_reason": list(self.handoff_reason),
-                "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks}
+                "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks,
+                "refine_solves": self.refine_solves, "refine_warp_steps": self.refine_warp_steps}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.

@@ -21,6 +21,17 @@ LIB = os.path.join(HERE, "libfrg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["frg_track.cu", "frg_track_team.cu", "frg_capi.cu", "frg_noalloc.cu"]
+# The tracking kernels' FP32 arithmetic is checked by residuals and finished in FP64,
+# so FP32 division and square root use the fast approximate forms (a few ulp) and FP32
+# subnormals flush to zero; FP64 arithmetic is unaffected by these flags.
+SOURCE_FLAGS = {"frg_track.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+                "frg_track_team.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]}
+STAMP = os.path.join(BUILD, "flags.txt")
+
+
+def _extra_flags() -> list:
+    """Additional nvcc flags for the CUDA sources from FRG_NVCC_FLAGS (space separated)."""
+    return os.environ.get("FRG_NVCC_FLAGS", "").split()
 CXX_SOURCES = ["frg_collect.cpp"]
 
 
@@ -42,7 +53,9 @@ def _sources_newer_than(target: str) -> bool:
 
 def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
     """Compile (if stale) and return the path of libfrg_gb300.so."""
-    if not force and not _sources_newer_than(LIB):
+    flags_id = " ".join(_extra_flags())
+    old_id = open(STAMP).read() if os.path.exists(STAMP) else ""
+    if not force and not _sources_newer_than(LIB) and old_id == flags_id:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -51,7 +64,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     jobs = []
     for src in CUDA_SOURCES:
         obj = os.path.join(BUILD, src + ".o")
-        cmd = [cc, *ARCH, *common, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *common, *SOURCE_FLAGS.get(src, []), *_extra_flags(), "-c", os.path.join(CSRC, src),
+               "-o", obj]
         if ptxas_info:
             cmd += ["-Xptxas", "-v"]
         jobs.append((cmd, obj))
@@ -82,6 +96,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(flags_id)
     return LIB
 
 

@@ -57,6 +57,7 @@ struct frg_ctx {
   int team_blocks_per_sm[3] = {0, 0, 0};
   std::string err;
   DevBuf fpm, gamma, fpm_lo, gamma_lo, fpm_df, gamma_df, task_start, queue, counters, roots, codes, yfinal, resid;
+  DevBuf starts;  // per-path start values (team kernels)
   DevBuf handoff, handoff_list, lo_lists;
   std::vector<cudaEvent_t> round_ev;  // events around the mixed-precision launches
   int last_rounds = 0;
@@ -105,6 +106,8 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->mixed_rounds = 1;
   c->lo_refine = 1;
   c->lo_endgame = 0;
+  c->path_offset = 0;
+  c->fp64_budget = 0;
   return FRG_OK;
 }
 
@@ -124,6 +127,8 @@ static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->kernel_variant != FRG_KERNEL_TEAM && c->kernel_variant != FRG_KERNEL_THREAD)
     return fail(ctx, FRG_ERR_ARG, "unknown kernel_variant");
   if (c->mixed_rounds < 0 || c->mixed_rounds > 64) return fail(ctx, FRG_ERR_ARG, "mixed_rounds must be in 0..64");
+  if (c->path_offset < 0) return fail(ctx, FRG_ERR_ARG, "path_offset must be non-negative");
+  if (c->fp64_budget < 0) return fail(ctx, FRG_ERR_ARG, "fp64_budget must be non-negative");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   return FRG_OK;
@@ -164,7 +169,7 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->fpm_df, &ctx->gamma_df,
+  for (DevBuf* b : {&ctx->starts, &ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->fpm_df, &ctx->gamma_df,
                     &ctx->task_start, &ctx->queue,
                     &ctx->counters, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->handoff,
                     &ctx->handoff_list, &ctx->lo_lists})
@@ -257,6 +262,12 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   a.work = nullptr;
   a.counters = (unsigned long long*)ctx->counters.p;
   const bool team = ctx->cfg.kernel_variant == FRG_KERNEL_TEAM;
+  if (team) {  // start values for every path, generated once up front
+    FRG_CUDA(ctx, ctx->starts.ensure(sizeof(cx<double>) * frg::FRG_START_STRIDE * (size_t)N));
+    a.starts = (const cx<double>*)ctx->starts.p;
+    cudaError_t e = frg_launch_starts(a, (cx<double>*)ctx->starts.p, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "start kernel launch");
+  }
   // persistent grids: SMs x resident blocks, capped by the work (one path per thread
   // for the thread kernels, one per 8 lanes for the team kernels)
   auto grid_for = [&](int mode, int64_t n) {
@@ -416,6 +427,8 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
         stats->stage_ms[1] += m1;
       }
       stats->handbacks = (int64_t)cnt[13];
+      stats->refine_solves = (int64_t)cnt[22];
+      stats->refine_warp_steps = (int64_t)cnt[23];
     } else {
       stats->stage_ms[1] = ms;
     }

@@ -6,8 +6,12 @@
 // Built from the error-free transformations two-sum (Knuth, TAOCP vol. 2, 4.2.2) and
 // two-product via a fused multiply-add (the FMA form of Dekker's product, T. J.
 // Dekker, "A floating-point technique for extending the available precision",
-// Numer. Math. 18, 1971); addition renormalises both components (the accurate,
-// cancellation-safe variant), division takes two quotient corrections.
+// Numer. Math. 18, 1971). Addition is Dekker's add2 (one two-sum of the leading parts,
+// the trailing parts added in, one renormalisation): its error is at most about
+// u^2 (|x| + |y|) with u = 2^-24, i.e. it perturbs each operand by a relative u^2, which is
+// the backward-error form the residuals and eliminations here rely on. The complex
+// operations evaluate a*b -/+ c*d with one two-sum of the two leading products and the
+// cross terms folded into the trailing part (error about u^2 (|a b| + |c d|)).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -36,12 +40,9 @@ __device__ __forceinline__ void df_quick_two_sum(float a, float b, float& s, flo
 }
 
 __device__ __forceinline__ df operator+(df x, df y) {
-  float s, e, t, f;
+  float s, e;
   df_two_sum(x.hi, y.hi, s, e);
-  df_two_sum(x.lo, y.lo, t, f);
-  e += t;
-  df_quick_two_sum(s, e, s, e);
-  e += f;
+  e += x.lo + y.lo;
   df_quick_two_sum(s, e, s, e);
   return df(s, e);
 }
@@ -82,3 +83,74 @@ __device__ __forceinline__ df sqrt(df a) {
 }
 __device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
 __device__ __forceinline__ df fmin(df a, df b) { return a < b ? a : b; }
+
+// ---------------------------------------------------------------- complex double-float
+#include "frg_complex.cuh"
+
+// a*b + sgn*c*d (sgn = +1 or -1), one renormalisation
+__device__ __forceinline__ df df_dot2(df a, df b, df c, df d, float sgn) {
+  const float p1 = a.hi * b.hi, e1 = fmaf(a.hi, b.hi, -p1);
+  const float cs = sgn * c.hi, cl = sgn * c.lo;
+  const float p2 = cs * d.hi, e2 = fmaf(cs, d.hi, -p2);
+  float s, t;
+  df_two_sum(p1, p2, s, t);
+  t += e1 + e2;
+  t = fmaf(a.hi, b.lo, t);
+  t = fmaf(a.lo, b.hi, t);
+  t = fmaf(cs, d.lo, t);
+  t = fmaf(cl, d.hi, t);
+  df_quick_two_sum(s, t, s, t);
+  return df(s, t);
+}
+// z + a*b + sgn*c*d
+__device__ __forceinline__ df df_dot2_acc(df z, df a, df b, df c, df d, float sgn) {
+  const float p1 = a.hi * b.hi, e1 = fmaf(a.hi, b.hi, -p1);
+  const float cs = sgn * c.hi, cl = sgn * c.lo;
+  const float p2 = cs * d.hi, e2 = fmaf(cs, d.hi, -p2);
+  float s, t, s2, t2;
+  df_two_sum(p1, p2, s, t);
+  df_two_sum(s, z.hi, s2, t2);
+  t += t2 + z.lo + e1 + e2;
+  t = fmaf(a.hi, b.lo, t);
+  t = fmaf(a.lo, b.hi, t);
+  t = fmaf(cs, d.lo, t);
+  t = fmaf(cl, d.hi, t);
+  df_quick_two_sum(s2, t, s2, t);
+  return df(s2, t);
+}
+// 1 / y: an approximate FP32 reciprocal with one correction from the exact residual
+__device__ __forceinline__ df df_rcp(df y) {
+  const float q1 = 1.0f / y.hi;
+  const float p = y.hi * q1, e = fmaf(y.hi, q1, -p);
+  const float r = ((1.0f - p) - e) - y.lo * q1;  // 1 - p is exact (Sterbenz)
+  const float q2 = r * q1;
+  float s, t;
+  df_quick_two_sum(q1, q2, s, t);
+  return df(s, t);
+}
+
+__device__ __forceinline__ cx<df> operator+(cx<df> a, cx<df> b) { return cx<df>(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ cx<df> operator-(cx<df> a, cx<df> b) { return cx<df>(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ cx<df> operator*(cx<df> a, cx<df> b) {
+  return cx<df>(df_dot2(a.re, b.re, a.im, b.im, -1.f), df_dot2(a.re, b.im, a.im, b.re, 1.f));
+}
+__device__ __forceinline__ cx<df> operator*(df s, cx<df> a) { return cx<df>(s * a.re, s * a.im); }
+__device__ __forceinline__ cx<df> operator*(cx<df> a, df s) { return cx<df>(s * a.re, s * a.im); }
+__device__ __forceinline__ cx<df>& operator+=(cx<df>& a, cx<df> b) { a = a + b; return a; }
+__device__ __forceinline__ cx<df>& operator-=(cx<df>& a, cx<df> b) { a = a - b; return a; }
+// a - b*c
+__device__ __forceinline__ cx<df> cfms(cx<df> a, cx<df> b, cx<df> c) {
+  return cx<df>(df_dot2_acc(a.re, -b.re, c.re, b.im, c.im, 1.f), df_dot2_acc(a.im, -b.re, c.im, b.im, c.re, -1.f));
+}
+// a + b*c
+__device__ __forceinline__ cx<df> cfma(cx<df> b, cx<df> c, cx<df> a) {
+  return cx<df>(df_dot2_acc(a.re, b.re, c.re, b.im, c.im, -1.f), df_dot2_acc(a.im, b.re, c.im, b.im, c.re, 1.f));
+}
+__device__ __forceinline__ df cnorm2(cx<df> a) { return df_dot2(a.re, a.re, a.im, a.im, 1.f); }
+// 1/b = conj(b) / |b|^2 (the tracker's operands are far from the FP32 range limits)
+__device__ __forceinline__ cx<df> cinv(cx<df> b) {
+  const df r = df_rcp(cnorm2(b));
+  return cx<df>(b.re * r, -(b.im * r));
+}
+__device__ __forceinline__ cx<df> cdiv(cx<df> a, cx<df> b) { return a * cinv(b); }
+

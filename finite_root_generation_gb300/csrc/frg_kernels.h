@@ -31,6 +31,8 @@ struct Handoff {
 };
 
 // Device-side arguments of one tracking launch. All arrays are device memory.
+constexpr int FRG_START_STRIDE = 51;
+
 struct TrackArgs {
   frg_config cfg;
   const cx<double>* fpm;        // ntasks x 30 target parameters
@@ -49,8 +51,9 @@ struct TrackArgs {
   cx<double>* yfinal;           // npaths x 23, optional
   double* resid;                // npaths, optional
   int32_t* work;                // npaths x 3 (ivp solves, newton iterations, steps), optional
-  unsigned long long* counters; // 24: codes[8], ivp, newton, steps, fp64 solves, handoffs, -, -,
-                                //     handoff reasons 1..6 at [16..21]
+  unsigned long long* counters; // 40: codes[8], ivp, newton, steps, fp64 solves, handoffs, hand-backs, -,
+                                //     handoff reasons 1..6 at [16..21], kernel cycles at [24..35]
+  const cx<double>* starts;     // npaths x FRG_START_STRIDE start values (null: generated inline)
   Handoff* handoff;             // npaths slots (mixed precision)
   int64_t* handoff_list;        // ids of paths handed to the FP64 kernel
   unsigned long long* handoff_count;
@@ -66,6 +69,9 @@ struct TrackArgs {
 cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
 cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_team(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream);
+// GenerateStart for every path into args.starts (FRG_START_STRIDE complex per path:
+// the 21 start unknowns, then the 30 start parameters)
+cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cudaStream_t stream);
 cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);
 cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream);

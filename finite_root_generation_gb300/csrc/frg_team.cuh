@@ -79,9 +79,9 @@ __device__ __forceinline__ T team_min(unsigned mask, T v) {
 }
 
 // Per-team shared state of one path. The points Yc (accepted), Yn (predicted) and
-// YN (corrector iterate) are FP64 in every mode, so corrector iterations of the FP32
-// stage refine in FP64 (FP64 residual, FP32 solve); directions, patches and
-// stage vectors are in the working precision T. U/Urhs hold the reduced system's
+// YN (corrector iterate) are in the point type (FP64, or double-float in the FP32
+// stage, whose corrector refines on double-float residuals with an FP32 solve);
+// directions, patches and stage vectors are in the working precision T. U/Urhs hold the reduced system's
 // upper factor for the back substitution. The 32-byte pad makes the stride between
 // teams 32 bytes past a multiple of 128, so the four teams of a warp reading "the
 // same" field hit different bank groups.
@@ -117,7 +117,7 @@ __device__ __forceinline__ int param_index(int slot, int j) {
 
 template <typename T>
 struct StepOut {
-  T ratio;   // pivot ratio max|u_ii| / min|u_ii| over all 23 pivots
+  T ratio;   // condition estimate (pivot ratios of the elimination), +inf if not finite
   T xnorm2;  // |x|^2 of the (normalised, for tangents) solution
   T hnorm;   // |H| at the evaluation point (Newton)
 };
@@ -169,14 +169,15 @@ __device__ __forceinline__ void lu_window_step(Smem<T>& S, int k, int g, cx<T>* 
 #pragma unroll
   for (int c = 0; c < W; ++c) prow[c] = shfl(FULL, ps ? R1[c] : R0[c], pl);
   const cx<T> prhs = shfl(FULL, ps ? R1r : R0r, pl);
-  if (g == 0) {
+  const cx<T> ip = cinv(prow[0]);
+  if (g == 0) {  // the diagonal keeps the pivot's reciprocal for the back substitution
+    S.U[k][k] = ip;
 #pragma unroll
-    for (int c = 0; c < W; ++c)
+    for (int c = 1; c < W; ++c)
       if (k + c < 16) S.U[k][k + c] = prow[c];
     S.Urhs[k] = prhs;
   }
-  const cx<T> ip = cinv(prow[0]);
-  const T pa = sqrt(cnorm2(prow[0]));
+  const T pa = cnorm2(prow[0]);  // squared pivot magnitude
   pmax = fmax(pmax, pa);
   pmin = fmin(pmin, pa);
   const cx<T> l0 = used0 ? zero : R0[0] * ip;
@@ -212,6 +213,9 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   const int j = grp ? g + 1 : 7;
   const cx<T> zero(T(0));
   constexpr bool LOWP = sizeof(T) < sizeof(double);
+  // `newton` and `hires` are per team, so reductions inside branches on them use the
+  // team's own mask; everything outside such branches runs on the full warp
+  const unsigned tmask = 0xffu << (threadIdx.x & 24);
 
   // ---- FP64 residual of the corrector (FP32 stage only)
   cx<T> hF0 = zero, hF1 = zero, hF2 = zero, hU = zero;
@@ -219,9 +223,10 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   if (LOWP && newton && hires) {
     cx<P> fI, fII, fIII;
     residual_hi<P>(S.YN, S.spm, fpm_hi, gamma_hi, j, fI, fII, fIII);
+    // patch residual u . YN - 1, its 23 terms spread over the team
     cx<P> d(P(0));
-    for (int e = 0; e < 23; ++e) d = cfma(cx<P>(S.u[e]), S.YN[e], d);
-    d = d - cx<P>(P(1));
+    for (int e = g; e < 23; e += TEAM) d = cfma(cx<P>(S.u[e]), S.YN[e], d);
+    d = cx<P>(team_sum(tmask, d.re), team_sum(tmask, d.im)) - cx<P>(P(1));
     hF0 = cx<T>(fI); hF1 = cx<T>(fII); hF2 = cx<T>(fIII); hU = cx<T>(d);
     hsq = grp ? T(cnorm2(hF0) + cnorm2(hF1) + cnorm2(hF2)) : T(cnorm2(hU));
   }
@@ -305,15 +310,13 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   // ---- patch rows (lane 7) and the folding of every group's pivot row into them
   const cx<T>* u = S.u;
   T su = T(0);
-#pragma unroll
-  for (int e = 0; e < 23; ++e) su = fmax(su, fmax(tabs(u[e].re), tabs(u[e].im)));
-  su = T(1) / su;
+  for (int e = g; e < 23; e += TEAM) su = fmax(su, fmax(tabs(u[e].re), tabs(u[e].im)));
+  su = T(1) / team_max(FULL, su);
   const T tdiff = tgoal - t;
-  if (lores_h && newton) {
+  if (lores_h && newton) {  // patch residual u . Ye - 1, its 23 terms spread over the team
     cx<T> d(T(0));
-#pragma unroll
-    for (int e = 0; e < 23; ++e) d = cfma(u[e], S.Ye[e], d);
-    hU = d - cx<T>(T(1));
+    for (int e = g; e < 23; e += TEAM) d = cfma(u[e], S.Ye[e], d);
+    hU = cx<T>(team_sum(tmask, d.re), team_sum(tmask, d.im)) - cx<T>(T(1));
   }
   if (!grp) {
     if (lores_h) hsq = cnorm2(hU);
@@ -346,6 +349,23 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
     R1r = (newton ? cx<T>(tdiff) : cx<T>(T(1))) - Sw[16];
   }
 
+  // ---- re-scale the 16 dense rows (max(|re|,|im|) = 1): eliminating U_j can shrink a
+  //      group row by cancellation, and unequal rows would mislead both the pivot
+  //      choice and the pivot-ratio condition estimate (with the re-scaling the ratio
+  //      tracks the reference's 23 x 23 row-scaled elimination)
+  {
+    T m0 = T(0), m1 = T(0);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      m0 = fmax(m0, fmax(tabs(R0[c].re), tabs(R0[c].im)));
+      m1 = fmax(m1, fmax(tabs(R1[c].re), tabs(R1[c].im)));
+    }
+    const T s0 = T(1) / m0, s1 = T(1) / m1;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) { R0[c] = s0 * R0[c]; R1[c] = s1 * R1[c]; }
+    R0r = s0 * R0r;
+    R1r = s1 * R1r;
+  }
   // ---- dense 16 x 16 LU with partial pivoting across the team: 8 steps over a
   //      16-wide window, then 8 over the remaining 8 columns
   bool used0 = false, used1 = false;
@@ -366,7 +386,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   __syncwarp();
 #pragma unroll 1
   for (int k = 15; k >= 0; --k) {
-    const cx<T> mine = ((k >> 3) ? rb1 : rb0) * cinv(S.U[k][k]);
+    const cx<T> mine = ((k >> 3) ? rb1 : rb0) * S.U[k][k];
     const cx<T> xk = shfl(FULL, mine, k & 7);
     if (g == 0) S.Urhs[k] = xk;
     if (g < k) rb0 = cfms(rb0, S.U[g][k], xk);
@@ -381,13 +401,14 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
 #pragma unroll
   for (int c = 0; c < 16; ++c) xu = cfms(xu, piv[c], xg[c]);
   xu = xu * ipu;
-  // ---- condition estimate: the pivot ratio over all 23 pivots. A small group pivot
-  //      (a U_j column weak in its group's rows, where a dense elimination would pivot
-  //      on a patch row) makes this elimination lose accuracy, so it counts too.
+  // ---- condition estimate: the larger of the dense phase's pivot ratio and the
+  //      worst group amplification 1/|u_jj| (a group's pivot row is row-scaled, so its
+  //      largest entry is about 1, and U_j's error grows like eps / |u_jj|). A
+  //      non-finite solution (zero or non-finite pivot) makes it infinite.
+  T ratio;
   {
-    const T gp = grp ? sqrt(cnorm2(piv[16])) : pmax;
-    pmax = fmax(pmax, team_max(FULL, gp));
-    pmin = fmin(pmin, team_min(FULL, grp ? gp : pmin));
+    const T ig = grp ? T(1) / cnorm2(piv[16]) : T(0);
+    ratio = sqrt(fmax(pmax / pmin, team_max(FULL, ig)));
   }
   // ---- normalisation and output
   T n2 = T(0);
@@ -396,7 +417,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   n2 += team_sum(FULL, grp ? cnorm2(xu) : T(0));
   StepOut<T> out;
   out.hnorm = sqrt(team_sum(FULL, hsq));
-  out.ratio = pmax / pmin;
+  out.ratio = (n2 - n2 == T(0)) ? ratio : T(INFINITY);  // n2 - n2 is NaN iff n2 is not finite
   if (!newton) {
     const cx<T> xt = xg[15];
     cx<T> sc;

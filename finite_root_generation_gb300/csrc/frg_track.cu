@@ -155,7 +155,7 @@ track_kernel(TrackArgs a) {
       P.task = lo;
       // Start system (frg.cu:54): the stream of path id; TrackPath receives the same
       // fresh state (frg.cu:57, by value), so its draws restart at index 0.
-      P.rng.seed = a.seed; P.rng.stream = (uint64_t)id; P.rng.index = 0;
+      P.rng.seed = a.seed; P.rng.stream = (uint64_t)(id + c.path_offset); P.rng.index = 0;
       cd spt[NV], spm[NP];
       generate_start(P.rng, c.start_dist, c.start_range, spt, spm);
 #pragma unroll 1

@@ -210,9 +210,13 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   const bool lo_resume = LO && a.lo_list != nullptr;
   const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count
                          : (lo_resume ? (int64_t)*a.lo_count : a.npaths);
-  // a path returns from FP64 to FP32 after this many consecutive well-conditioned solves
+  // A path returns from FP64 to the next round's FP32 kernel after kBackSteps
+  // consecutive well-conditioned solves, or after kSegment FP64 solves in this launch
+  // (FP64 latency per solve is high on this part, so long FP64 segments set a launch's
+  // tail; a path still ill conditioned is simply handed over again by the FP32 kernel).
   constexpr int kBackSteps = 16;
-  constexpr int kMaxBounces = 8;
+  constexpr int kSegment = 96;
+  constexpr int kMaxBounces = 64;
 
   LaneParams<T> lp;
   int64_t id = -1;
@@ -224,12 +228,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   int phase = PH_FETCH;
   bool hires = !LO;
   T res_prev = T(0);
-  int good = 0, bounces = 0;
+  int good = 0, bounces = 0, seg = 0;
   unsigned long long fp64_solves = 0;
   // cycle accounting (lane 0 of each warp): fetch, setup, linear step, transitions;
   // warp steps and active-team steps
   long long cyc[4] = {0, 0, 0, 0};
-  long long warp_steps = 0, team_steps = 0;
+  long long warp_steps = 0, team_steps = 0, refine_steps = 0, refine_warp = 0;
   __syncwarp();
 
   for (;;) {
@@ -249,7 +253,15 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       task = lo;
       {
         cd z[14], Uj, sp[6];
-        team_start(a.seed, (uint64_t)id, c.start_dist, c.start_range, jg, z, Uj, sp);
+        if (a.starts) {  // precomputed by the start kernel: lane g reads what team_start gives it
+          const cd* st = a.starts + (size_t)id * FRG_START_STRIDE;
+          for (int e = g; e < 14; e += TEAM) z[e] = st[e];
+          Uj = st[13 + jg];
+#pragma unroll
+          for (int i = 0; i < 6; ++i) sp[i] = st[21 + param_index(i, jg)];
+        } else {
+          team_start(a.seed, (uint64_t)(id + c.path_offset), c.start_dist, c.start_range, jg, z, Uj, sp);
+        }
         const cx<T>* fpmT = fpm_of<T>(a, task);
 #pragma unroll
         for (int i = 0; i < 6; ++i) { lp.sp[i] = cx<T>(sp[i]); lp.fp[i] = fpmT[param_index(i, jg)]; }
@@ -265,7 +277,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         }
       }
       code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
-      good = 0; bounces = 0;
+      good = 0; bounces = 0; seg = 0;
       if (MODE == MODE_RESUME || lo_resume) {
         const Handoff& h = a.handoff[id];
         for (int e = g; e < NY; e += TEAM) {
@@ -289,11 +301,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         // TrackPath's patches start at draw 0 of the path's stream (by-value state,
         // frg.cu:54,57); u (htpytrack.cu:53-58) then the random velocity patch (:63-67).
         const double R = c.patch_range;
+        const uint64_t stream = (uint64_t)(id + c.path_offset);
         for (int e = g; e < NY; e += TEAM) {
-          S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, 2 * e) - R),
-                         T(2.0 * R * frg_uniform01(a.seed, id, 2 * e + 1) - R));
-          S.Vc[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, 46 + 2 * e) - R),
-                          T(2.0 * R * frg_uniform01(a.seed, id, 47 + 2 * e) - R));
+          S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, 2 * e) - R),
+                         T(2.0 * R * frg_uniform01(a.seed, stream, 2 * e + 1) - R));
+          S.Vc[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, 46 + 2 * e) - R),
+                          T(2.0 * R * frg_uniform01(a.seed, stream, 47 + 2 * e) - R));
         }
         rng_index = 92;
         __syncwarp(tmask);
@@ -353,10 +366,17 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     {
       const unsigned act = __ballot_sync(FULL, phase != PH_IDLE && g == 0);
       if (lane == 0) team_steps += __popc(act);
+      if (LO) {  // corrector iterations on double-float residuals, and warp steps that ran one
+        const unsigned ref = __ballot_sync(FULL, phase != PH_IDLE && g == 0 && newton && hires);
+        if (lane == 0) { refine_steps += __popc(ref); refine_warp += ref != 0u; }
+      }
     }
     if (phase == PH_IDLE) continue;
     if (!LO) ++fp64_solves;
-    if (MODE == MODE_RESUME) good = (r.ratio < T(c.cond_switch * 1e-2)) ? good + 1 : 0;
+    if (MODE == MODE_RESUME) {
+      good = (r.ratio < T(c.cond_switch * 1e-2)) ? good + 1 : 0;
+      ++seg;
+    }
     if (newton) ++n_newton; else ++n_ivp;
 
     // ============================================= transitions (per team)
@@ -366,6 +386,9 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     bool final_from_YN = false;
     if (LO && !(r.ratio <= T(c.cond_switch))) {
       handoff = 2;  // ill-conditioned (or non-finite) step: continue in FP64 from Yc
+    } else if (MODE == MODE_RESUME && c.fp64_budget > 0 && seg >= c.fp64_budget) {
+      code = 2;  // the FP64 budget of this path is spent: retire it as a step-limit failure
+      finished = true;
     } else if (phase == PH_TANGENT0) {
       for (int e = g; e < NY; e += TEAM) S.Vc[e] = S.dx[e];
       if (c.max_steps == 0) { code = 1; finished = true; }
@@ -465,8 +488,9 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
             step++;
             if (step == c.max_steps) { code = 1; finished = true; }
             else if (LO && !c.lo_endgame && double(S.YN[22].re) >= c.t_switch) handoff = 1;
-            else if (MODE == MODE_RESUME && a.back_list && good >= kBackSteps && bounces < kMaxBounces &&
-                     double(S.YN[22].re) < c.t_switch) handback = true;  // well conditioned again: back to FP32
+            else if (MODE == MODE_RESUME && a.back_list && (good >= kBackSteps || seg >= kSegment) &&
+                     bounces < kMaxBounces && (c.lo_endgame || double(S.YN[22].re) < c.t_switch))
+              handback = true;  // back to FP32 (well conditioned again, or the segment is used up)
             else { stage = 0; phase = PH_RK; }
           }
         } else if (ok && sharp) {
@@ -474,9 +498,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         } else {
           // new random patch and SwitchPatch(u, Yn, Yn) (htpytrack.cu:145-151, :204-210)
           const double R = c.patch_range;
+          const uint64_t stream = (uint64_t)(id + c.path_offset);
           for (int e = g; e < NY; e += TEAM)
-            S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, id, rng_index + 2 * e) - R),
-                           T(2.0 * R * frg_uniform01(a.seed, id, rng_index + 2 * e + 1) - R));
+            S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, rng_index + 2 * e) - R),
+                           T(2.0 * R * frg_uniform01(a.seed, stream, rng_index + 2 * e + 1) - R));
           rng_index += 46;
           __syncwarp(tmask);
           cp d(P(0));
@@ -559,11 +584,43 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     for (int i = 0; i < 4; ++i) atomicAdd(&a.counters[base + i], (unsigned long long)cyc[i]);
     atomicAdd(&a.counters[base + 4], (unsigned long long)warp_steps);
     atomicAdd(&a.counters[base + 5], (unsigned long long)team_steps);
+    if (LO) {
+      atomicAdd(&a.counters[22], (unsigned long long)refine_steps);
+      atomicAdd(&a.counters[23], (unsigned long long)refine_warp);
+    }
   }
 }
 
 }  // namespace team
 }  // namespace frg
+
+namespace frg {
+namespace team {
+// GenerateStart per path, one team per path (the same lane split as the tracking
+// kernels' inline generation, so the values are identical).
+__global__ void __launch_bounds__(FRG_TEAM_THREADS) start_kernel(TrackArgs a, cd* starts) {
+  const int g = threadIdx.x & 7;
+  const int64_t id = ((int64_t)blockIdx.x * FRG_TEAM_THREADS + threadIdx.x) >> 3;
+  if (id >= a.npaths) return;
+  const int jg = g < 7 ? g + 1 : 7;
+  cd z[14], Uj, sp[6];
+  team_start(a.seed, (uint64_t)(id + a.cfg.path_offset), a.cfg.start_dist, a.cfg.start_range, jg, z, Uj, sp);
+  cd* st = starts + (size_t)id * FRG_START_STRIDE;
+  for (int e = g; e < 14; e += TEAM) st[e] = z[e];
+  if (g < 7) {
+    st[13 + jg] = Uj;
+    st[21 + jg] = sp[2]; st[21 + 8 + jg] = sp[3]; st[21 + 15 + jg] = sp[4]; st[21 + 22 + jg] = sp[5];
+  }
+  if (g == 0) { st[21] = sp[0]; st[21 + 8] = sp[1]; }
+}
+}  // namespace team
+}  // namespace frg
+
+cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cudaStream_t stream) {
+  const int64_t blocks = (args.npaths * 8 + FRG_TEAM_THREADS - 1) / FRG_TEAM_THREADS;
+  frg::team::start_kernel<<<(unsigned)blocks, FRG_TEAM_THREADS, 0, stream>>>(args, starts);
+  return cudaGetLastError();
+}
 
 namespace {
 template <int MODE, typename T>

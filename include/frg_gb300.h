@@ -94,6 +94,10 @@ typedef struct frg_config {
                             newt_tol; 0 = it stops at newt_tol_lo */
   int lo_endgame;        /* mixed: 1 = the FP32 stage (with refinement) also runs the endgame and
                             sharpening, FP64 only for ill-conditioned steps; 0 = FP64 from t_switch */
+  int64_t path_offset;   /* random stream of local path i is path_offset + i: shards of one round
+                            (path-index ranges on several GPUs) reproduce the single-GPU round */
+  int fp64_budget;       /* mixed: a path that spends more FP64 solves than this in one FP64 launch
+                            ends with code 2 (step limit); 0 = no limit */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */
@@ -114,6 +118,8 @@ typedef struct frg_stats {
                                 kernel; per kernel the cycles in path fetch, step set-up, linear steps
                                 and transitions, then warp steps and active-team steps */
   int64_t handbacks;       /* mixed: returns from FP64 to FP32 once well conditioned again */
+  int64_t refine_solves;   /* mixed: FP32-stage corrector iterations on double-float residuals */
+  int64_t refine_warp_steps; /* mixed: FP32-stage warp steps in which at least one path refined */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;

@@ -148,3 +148,26 @@ def test_team_matches_thread_kernel():
     same = (b.codes[ok] == 0) & (_rel(b.roots[ok], a.roots[ok]) < ROOT_RTOL)
     assert same.mean() >= 0.99
     assert np.all(b.resid[b.codes == 0] <= 1e-10)
+
+
+def test_sharded_round_matches_single(tracker):
+    """A round split into path ranges (path_offset = the range's first global index,
+    every task kept at its global index) reproduces the single round path for path."""
+    from finite_root_generation_gb300 import shard
+
+    fpm = np.stack([precision_point_task(5, "disk"), precision_point_task(6, "curve")])
+    ppt = [40, 56]
+    whole = tracker.track(fpm, ppt, 77)
+    cfg0 = tracker.config
+    parts = []
+    try:
+        for r in range(3):
+            _, res = shard.track_shard(tracker, fpm, ppt, 77, r, 3, want_resid=False)
+            parts.append(res)
+    finally:
+        cfg0.path_offset = 0
+        tracker.set_config(cfg0)
+    codes = np.concatenate([p.codes for p in parts])
+    roots = np.concatenate([p.roots for p in parts])
+    assert np.array_equal(codes, whole.codes)
+    assert np.array_equal(roots, whole.roots)
