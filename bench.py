@@ -209,31 +209,40 @@ def flops_per_solve():
 
 
 # ---------------------------------------------------------------------- our impl
-def _timed_steps(torch, tracker, n, seeds, d_fpm, outs, flush, world):
-    """Run one step per seed, step i writing into outs[i] (device buffers), timed as one
-    region with CUDA events bracketed by a barrier and a synchronize on both sides.
-    L2 is flushed (a 256 MB write) before every step. Returns (ms, per-step stats)."""
+def _chosen_overrides():
+    """The chosen configuration on top of the workload's: mixed precision, the FP32
+    stage also running the endgame and sharpening (double-float refinement), FP64 for
+    steps whose condition estimate exceeds 1e5 and for finishing every root."""
+    return dict(mixed_rounds=1, lo_endgame=1, cond_switch=1e5, lo_points=1)
+
+
+def _round_sets(roots, codes, resid, n, k):
+    from finite_root_generation_gb300.metrics import distinct_roots
+    R = roots.cpu().numpy().view(np.complex128)
+    C = codes.cpu().numpy()
+    E = resid.cpu().numpy()
+    return [distinct_roots(R[i * n:(i + 1) * n], C[i * n:(i + 1) * n], E[i * n:(i + 1) * n], RESID_MAX)
+            for i in range(k)]
+
+
+def _timed_rounds(torch, tracker, d_fpm, n, seeds, outs, depth, world):
+    """K rounds through frg_track_rounds (device buffers, `depth` rounds in flight),
+    bracketed by a barrier and a synchronize on both sides. The library times the
+    span with CUDA events on its launching streams (first launch to the last round's
+    end); torch events on the current stream bracket the call as a cross-check."""
+    roots, codes, resid = outs
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
-    stats = []
-    for sd, (roots, codes, resid) in zip(seeds, outs):
-        flush.zero_()
-        stats.append(tracker.track_into(d_fpm, [n], sd, roots, codes, resid=resid))
+    st = tracker.track_rounds(d_fpm, [n], seeds, roots, codes, resid=resid, depth=depth)
     ev1.record()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    return ev0.elapsed_time(ev1), stats
-
-
-def _distinct_sets(outs):
-    from finite_root_generation_gb300.metrics import distinct_roots
-    return [distinct_roots(r.cpu().numpy().view(np.complex128), c.cpu().numpy(), e.cpu().numpy(), RESID_MAX)
-            for r, c, e in outs]
+    return st, ev0.elapsed_time(ev1)
 
 
 def run_ours(args, rank, world):
@@ -248,55 +257,60 @@ def run_ours(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     task = precision_point_task(TASK_SEED, "disk")
-    n = args.paths
-    chosen = frg.Tracker(workload_config(frg, frg.PREC_MIXED), device=dev)
+    n, k, depth = args.paths, args.steps, args.depth
+    chosen_cfg = workload_config(frg, frg.PREC_MIXED)
+    for key, v in _chosen_overrides().items():
+        setattr(chosen_cfg, key, v)
+    chosen = frg.Tracker(chosen_cfg, device=dev)
     plain = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
     d_fpm = torch.from_numpy(task.view(np.float64).copy()).cuda()
-
-    def out_bufs(k):
-        return [(torch.empty((n, 42), dtype=torch.float64, device="cuda"),
-                 torch.empty(n, dtype=torch.int32, device="cuda"),
-                 torch.empty(n, dtype=torch.float64, device="cuda")) for _ in range(k)]
-
-    outs = out_bufs(args.steps)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    nbuf = max(k, args.warmup, 1) * n
+    outs = (torch.empty((nbuf, 42), dtype=torch.float64, device="cuda"),
+            torch.empty(nbuf, dtype=torch.int32, device="cuda"),
+            torch.empty(nbuf, dtype=torch.float64, device="cuda"))
 
     def seed_of(step):
         return 1000003 * (rank + 1) + step
 
-    for w in range(args.warmup):
-        chosen.track_into(d_fpm, [n], seed_of(-1 - w), *outs[0][:2], resid=outs[0][2])
-    plain.track_into(d_fpm, [min(n, 8192)], seed_of(-1), *outs[0][:2], resid=outs[0][2])
+    seeds = [seed_of(i) for i in range(k)]
+    # warm-up: W rounds of the chosen configuration and one of the plain one
+    warm = [seed_of(-1 - i) for i in range(args.warmup)]
+    chosen.track_rounds(d_fpm, [n], warm, outs[0][: len(warm) * n], outs[1][: len(warm) * n],
+                        resid=outs[2][: len(warm) * n], depth=depth)
+    plain.track_rounds(d_fpm, [min(n, 8192)], warm[:1], outs[0], outs[1], resid=outs[2], depth=1)
     torch.cuda.synchronize()
 
     # ---- chosen configuration, inputs resident in HBM (value) ----
-    seeds = [seed_of(k) for k in range(args.steps)]
+    c_outs = tuple(o[: k * n] for o in outs)
     with ClockSampler(dev) as clk:
-        track_ms, c_stats = _timed_steps(torch, chosen, n, seeds, d_fpm, outs, flush, world)
+        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_fpm, n, seeds, c_outs, depth, world)
     clocks = clk.summary()
-    c_sets = _distinct_sets(outs)
-    # ---- plain FP64 on the same seeds (ratio and recall) ----
-    p_seeds = seeds[: max(1, args.plain_steps)]
-    p_outs = outs[: len(p_seeds)]
-    p_ms, p_stats = _timed_steps(torch, plain, n, p_seeds, d_fpm, p_outs, flush, world)
-    p_sets = _distinct_sets(p_outs)
-    rec = [recall(p_sets[i], c_sets[i]) for i in range(len(p_seeds))]
+    c_sets = _round_sets(*c_outs, n, k)
+    # ---- plain FP64 on the same seeds, pipelined the same way (ratio and recall) ----
+    kp = max(1, min(args.plain_steps, k))
+    p_st, _ = _timed_rounds(torch, plain, d_fpm, n, seeds[:kp], tuple(o[: kp * n] for o in outs), depth, world)
+    p_sets = _round_sets(*(o[: kp * n] for o in outs), n, kp)
+    rec = [recall(p_sets[i], c_sets[i]) for i in range(kp)]
 
-    # ---- end to end through the C ABI with host buffers (e2e) ----
-    h_roots = np.zeros((n, 21), np.complex128)
-    h_codes = np.zeros(n, np.int32)
-    h_resid = np.zeros(n, np.float64)
-    e2e_distinct = 0
+    # ---- end to end through the C ABI with pinned host buffers (e2e): per round the
+    #      task upload, tracking, the copy of roots/codes/residuals back, and the host
+    #      duplicate merge of every round ----
+    h_roots = torch.empty((k * n, 42), dtype=torch.float64, pin_memory=True)
+    h_codes = torch.empty(k * n, dtype=torch.int32, pin_memory=True)
+    h_resid = torch.empty(k * n, dtype=torch.float64, pin_memory=True)
+    hr, hc, he = h_roots.numpy(), h_codes.numpy(), h_resid.numpy()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for sd in seeds:
-        chosen.track_into(task, [n], sd, h_roots, h_codes, resid=h_resid)
-        e2e_distinct += len(distinct_roots(h_roots, h_codes, h_resid, RESID_MAX))
-    torch.cuda.synchronize()
+    chosen.track_rounds(task, [n], seeds, hr, hc, resid=he, depth=depth)
+    R = hr.view(np.complex128)
+    e2e_distinct = sum(len(distinct_roots(R[i * n:(i + 1) * n], hc[i * n:(i + 1) * n], he[i * n:(i + 1) * n],
+                                          RESID_MAX)) for i in range(k))
     e2e_s = time.perf_counter() - t0
 
+    track_ms = c_st["track_ms"]
+    p_ms = p_st["track_ms"]
     distinct = sum(len(d) for d in c_sets)
     p_distinct = sum(len(d) for d in p_sets)
     t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct], dtype=torch.float64)
@@ -315,30 +329,29 @@ def run_ours(args, rank, world):
     value = distinct / (track_ms * 1e-3)
     value_plain = p_distinct / (p_ms * 1e-3)
     e2e = e2e_distinct / e2e_s
-    # roofline of each kernel: algorithmic FLOPs per launch / launch time
+    # roofline of each kernel: algorithmic FLOPs of its launches / their CUDA-event time
     peaks = measure_fma_peaks()
     fps = flops_per_solve()
-    k = args.steps
-    solves = sum(st["ivp_solves"] + st["newton_iters"] for st in c_stats) / k
-    fp64_solves = sum(st["fp64_solves"] for st in c_stats) / k
+    solves = c_st["ivp_solves"] + c_st["newton_iters"]
+    fp64_solves = c_st["fp64_solves"]
     fp32_solves = solves - fp64_solves
-    ms32 = sum(st["stage_ms"][0] for st in c_stats) / k
-    ms64 = sum(st["stage_ms"][1] for st in c_stats) / k
+    ms32 = c_st["stage_ms"][0] / k
+    ms64 = c_st["stage_ms"][1] / k
     kernels = {
         "team_kernel<MODE_LO, float> (FP32 stage)": {
-            "bound": "fp32", "achieved": fp32_solves * fps / (ms32 * 1e-3) / 1e12, "peak": peaks["fp32"],
-            "ms_per_launch": ms32, "solves_per_launch": fp32_solves},
+            "bound": "fp32", "achieved": fp32_solves / k * fps / (ms32 * 1e-3) / 1e12, "peak": peaks["fp32"],
+            "ms_per_launch": ms32, "solves_per_launch": fp32_solves / k},
         "team_kernel<MODE_RESUME, double> (FP64 stage)": {
-            "bound": "fp64", "achieved": fp64_solves * fps / (ms64 * 1e-3) / 1e12, "peak": peaks["fp64"],
-            "ms_per_launch": ms64, "solves_per_launch": fp64_solves},
+            "bound": "fp64", "achieved": fp64_solves / k * fps / (ms64 * 1e-3) / 1e12, "peak": peaks["fp64"],
+            "ms_per_launch": ms64, "solves_per_launch": fp64_solves / k},
     }
     for v in kernels.values():
         v["frac"] = v["achieved"] / v["peak"]
     dom_name = max(kernels, key=lambda kk: kernels[kk]["ms_per_launch"])
     dom = kernels[dom_name]
-    p_solves = sum(st["ivp_solves"] + st["newton_iters"] for st in p_stats) / len(p_stats)
-    p_ms_launch = p_ms / len(p_stats)
-    plain_roof = p_solves * fps / (p_ms_launch * 1e-3) / 1e12
+    p_solves = (p_st["ivp_solves"] + p_st["newton_iters"]) / kp
+    p_ms_round = p_st["stage_ms"][1] / kp
+    plain_roof = p_solves * fps / (p_ms_round * 1e-3) / 1e12
     h2d = 16 * 30 + 16 + 16
     d2h = n * (16 * 21 + 4 + 8)
     line = {
@@ -346,18 +359,24 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": round(track_ms / k, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded task and start mechanisms)",
-        "config": {"workload": f"Stephenson II FRG round: {n} paths on 1 generic complex precision-point task "
-                               f"(seed {TASK_SEED}), complex-normal start mechanisms, random unit gamma; "
-                               "sharpening to 1e-12 in FP64, canonical cognates, finite + residual <= 1e-10 "
-                               "checks, duplicate removal",
-                   "paths_per_step": n, "chosen": "mixed precision (FP32 team stage, FP64 endgame), team kernels",
-                   "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{world}"},
-        "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": len(p_seeds),
-                       "ms_per_step": round(p_ms_launch, 3),
+        "config": {"workload": f"Stephenson II FRG rounds of {n} paths on 1 generic complex precision-point task "
+                               f"(seed {TASK_SEED}), complex-normal start mechanisms, random unit gamma per round; "
+                               "FP64 sharpening check, canonical cognates, finite + residual <= 1e-10 checks, "
+                               "duplicate removal",
+                   "paths_per_step": n, "rounds_in_flight": depth,
+                   "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
+                             "sharpening included), FP64 team kernel for steps with condition estimate > 1e5 "
+                             "and for finishing",
+                   "l2": "not flushed: per-round state (start values 816 B, hand-off record 1.2 KB, outputs "
+                         "348 B per path: ~155 MB per round, two rounds in flight) exceeds the 129 MB L2",
+                   "parallelism": f"replicas x{world}"},
+        "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": kp,
+                       "ms_per_step": round(p_ms / kp, 3),
                        "roofline_frac_fp64": round(plain_roof / peaks["fp64"], 4)},
         "speedup_vs_plain_fp64": round(value / value_plain, 3),
         "recall_vs_plain_fp64": round(min(rec), 5),
         "distinct_roots_per_step": distinct / k / world,
+        "torch_event_ms": round(c_torch_ms, 1),
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": dom_name, "bound": dom["bound"], "achieved": round(dom["achieved"], 4),
                      "peak": round(dom["peak"], 4), "unit": "TFLOP/s", "frac": round(dom["frac"], 4),
@@ -367,9 +386,9 @@ def run_ours(args, rank, world):
                      "flops_per_solve": fps,
                      "kernels": {kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
                                  for kk, v in kernels.items()}},
-        # per step: two conversions of the task parameters (FP32, double-float), then
-        # per mixed round one FP32-stage and one FP64-stage tracking kernel
-        "gpu_launches": (2 + 2 * max(1, chosen_rounds)) * k,
+        # per round: start values, FP32 and double-float parameter copies, then per mixed
+        # round one FP32-stage and one FP64-stage tracking kernel
+        "gpu_launches": (3 + 2 * max(1, chosen_rounds)) * k,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -439,11 +458,12 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--paths", type=int, default=65536)
     ap.add_argument("--cpu-sample", type=int, default=8192)
-    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--depth", type=int, default=3, help="rounds in flight")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -59,7 +59,7 @@ class FrgConfig(ctypes.Structure):
         ("threads_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
         ("newt_tol_lo", ctypes.c_double), ("kernel_variant", ctypes.c_int),
         ("mixed_rounds", ctypes.c_int), ("lo_refine", ctypes.c_int), ("lo_endgame", ctypes.c_int),
-        ("path_offset", ctypes.c_int64), ("fp64_budget", ctypes.c_int),
+        ("path_offset", ctypes.c_int64), ("fp64_budget", ctypes.c_int), ("lo_points", ctypes.c_int),
     ]
 
 
@@ -73,6 +73,8 @@ class FrgStats(ctypes.Structure):
         ("stage_ms", ctypes.c_double * 2), ("handoff_reason", ctypes.c_int64 * 6),
         ("kernel_cycles", ctypes.c_int64 * 12), ("handbacks", ctypes.c_int64),
         ("refine_solves", ctypes.c_int64), ("refine_warp_steps", ctypes.c_int64),
+        ("round_ms", ctypes.c_double * 32), ("fp64_segment_hist", ctypes.c_int64 * 6),
+        ("fp64_segment_max", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -81,7 +83,9 @@ class FrgStats(ctypes.Structure):
                 "track_ms": self.track_ms, "total_ms": self.total_ms, "handoffs": self.handoffs,
                 "stage_ms": list(self.stage_ms), "handoff_reason": list(self.handoff_reason),
                 "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks,
-                "refine_solves": self.refine_solves, "refine_warp_steps": self.refine_warp_steps}
+                "refine_solves": self.refine_solves, "refine_warp_steps": self.refine_warp_steps,
+                "round_ms": list(self.round_ms), "fp64_segment_hist": list(self.fp64_segment_hist),
+                "fp64_segment_max": self.fp64_segment_max}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.
@@ -89,7 +93,7 @@ EXPORTS = [
     "frg_config_default", "frg_create", "frg_destroy", "frg_last_error", "frg_set_config", "frg_track",
     "frg_track_async", "frg_coll_create", "frg_coll_destroy", "frg_coll_size", "frg_coll_get", "frg_coll_merge",
     "frg_coll_save", "frg_coll_load", "frg_codes_append", "frg_lambertw0", "frg_estimate_collected",
-    "frg_track_noalloc",
+    "frg_track_noalloc", "frg_track_rounds",
 ]
 NOALLOC_MAX_TASKS = 1024
 
@@ -118,6 +122,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_track_async.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _I64, ctypes.c_uint64,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p]
+    lib.frg_track_rounds.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _I64, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(FrgStats)]
     lib.frg_destroy.argtypes = [ctypes.c_void_p]
     lib.frg_last_error.argtypes = [ctypes.c_void_p]
     lib.frg_set_config.argtypes = [ctypes.c_void_p, ctypes.POINTER(FrgConfig)]
@@ -231,6 +238,18 @@ class Tracker:
         st = self.lib.frg_track(self._ctx, _ptr(fpm), len(ppt), ppt.ctypes.data_as(_I64), ctypes.c_uint64(seed),
                                 _ptr(roots), _ptr(codes), _ptr(yfinal), _ptr(resid), ctypes.byref(stats))
         self._check(st, "frg_track")
+        return stats.as_dict()
+
+    def track_rounds(self, fpm, paths_per_task, seeds, roots, codes, resid=None, depth: int = 2) -> dict:
+        """Track len(seeds) rounds, up to `depth` in flight (frg_track_rounds); outputs are
+        [rounds * N, ...] buffers, all numpy host arrays or all torch CUDA tensors."""
+        ppt = np.ascontiguousarray(np.atleast_1d(np.asarray(paths_per_task, dtype=np.int64)))
+        sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
+        stats = FrgStats()
+        st = self.lib.frg_track_rounds(self._ctx, _ptr(fpm), len(ppt), ppt.ctypes.data_as(_I64), len(sd),
+                                       sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), int(depth), _ptr(roots),
+                                       _ptr(codes), _ptr(resid), ctypes.byref(stats))
+        self._check(st, "frg_track_rounds")
         return stats.as_dict()
 
     def track_async(self, fpm, paths_per_task, seed: int, roots, codes, yfinal=None, resid=None, stream=0):

@@ -47,6 +47,25 @@ bool is_device_ptr(const void* p) {
 
 }  // namespace
 
+namespace {
+// Buffers of one round in flight: a round's launches use only its slot, so rounds on
+// different slots (different streams) run concurrently.
+struct Slot {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DevBuf gamma, gamma_lo, gamma_df, fpm_lo, fpm_df, task_start, queue, counters, starts;
+  DevBuf handoff, handoff_list, lo_lists;
+  DevBuf roots, codes, resid;  // staging of host outputs (frg_track_rounds)
+  void release() {
+    for (DevBuf* b : {&gamma, &gamma_lo, &gamma_df, &fpm_lo, &fpm_df, &task_start, &queue, &counters, &starts,
+                      &handoff, &handoff_list, &lo_lists, &roots, &codes, &resid})
+      b->release();
+    if (own_stream && stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+};
+}  // namespace
+
 struct frg_ctx {
   int device = 0;
   frg_config cfg;
@@ -54,13 +73,14 @@ struct frg_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evmid = nullptr;
   int sm_count = 0;
   int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each thread-per-path kernel mode
-  int team_blocks_per_sm[3] = {0, 0, 0};
+  int team_blocks_per_sm[4] = {0, 0, 0, 0};
   std::string err;
-  DevBuf fpm, gamma, fpm_lo, gamma_lo, fpm_df, gamma_df, task_start, queue, counters, roots, codes, yfinal, resid;
-  DevBuf starts;  // per-path start values (team kernels)
-  DevBuf handoff, handoff_list, lo_lists;
-  std::vector<cudaEvent_t> round_ev;  // events around the mixed-precision launches
+  DevBuf fpm, roots, codes, yfinal, resid;
+  std::vector<Slot*> slots;           // slot 0 runs on `stream`
+  std::vector<cudaEvent_t> round_ev;  // events around the mixed-precision launches of frg_track
   int last_rounds = 0;
+  unsigned long long* h_counters = nullptr;  // pinned per-round counter copies (frg_track_rounds)
+  size_t h_counters_n = 0;
 };
 
 static frg_status fail(frg_ctx* ctx, frg_status s, const std::string& msg) {
@@ -108,6 +128,7 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->lo_endgame = 0;
   c->path_offset = 0;
   c->fp64_budget = 0;
+  c->lo_points = 0;
   return FRG_OK;
 }
 
@@ -129,6 +150,8 @@ static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->mixed_rounds < 0 || c->mixed_rounds > 64) return fail(ctx, FRG_ERR_ARG, "mixed_rounds must be in 0..64");
   if (c->path_offset < 0) return fail(ctx, FRG_ERR_ARG, "path_offset must be non-negative");
   if (c->fp64_budget < 0) return fail(ctx, FRG_ERR_ARG, "fp64_budget must be non-negative");
+  if (c->lo_refine < 0 || c->lo_refine > 2) return fail(ctx, FRG_ERR_ARG, "lo_refine must be 0, 1 or 2");
+  if (c->lo_points < 0 || c->lo_points > 1) return fail(ctx, FRG_ERR_ARG, "lo_points must be 0 or 1");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   return FRG_OK;
@@ -157,6 +180,13 @@ extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int devic
     if (e == cudaSuccess) e = frg_team_occupancy(m, &ctx->team_blocks_per_sm[m]);
     if (ctx->team_blocks_per_sm[m] < 1) ctx->team_blocks_per_sm[m] = 1;
   }
+  if (e == cudaSuccess) e = frg_team_occupancy(3, &ctx->team_blocks_per_sm[3]);
+  if (ctx->team_blocks_per_sm[3] < 1) ctx->team_blocks_per_sm[3] = 1;
+  if (e == cudaSuccess) {
+    Slot* s0 = new (std::nothrow) Slot();
+    if (!s0) e = cudaErrorMemoryAllocation;
+    else { s0->stream = ctx->stream; ctx->slots.push_back(s0); }
+  }
   if (e != cudaSuccess) {
     frg_destroy(ctx);
     return FRG_ERR_CUDA;
@@ -169,11 +199,13 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->starts, &ctx->fpm, &ctx->gamma, &ctx->fpm_lo, &ctx->gamma_lo, &ctx->fpm_df, &ctx->gamma_df,
-                    &ctx->task_start, &ctx->queue,
-                    &ctx->counters, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->handoff,
-                    &ctx->handoff_list, &ctx->lo_lists})
-    b->release();
+  for (Slot* sl : ctx->slots) {
+    if (sl->stream) cudaStreamSynchronize(sl->stream);
+    sl->release();
+    delete sl;
+  }
+  for (DevBuf* b : {&ctx->fpm, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid}) b->release();
+  if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->round_ev) cudaEventDestroy(e);
@@ -192,6 +224,19 @@ extern "C" frg_status frg_set_config(frg_ctx* ctx, const frg_config* cfg) {
   return FRG_OK;
 }
 
+static int mixed_rounds_of(const frg_config& c) {
+  return c.kernel_variant == FRG_KERNEL_TEAM ? (c.mixed_rounds > 0 ? c.mixed_rounds : 1) : 1;
+}
+
+static frg_status ensure_events(frg_ctx* ctx, std::vector<cudaEvent_t>& v, size_t n) {
+  while (v.size() < n) {
+    cudaEvent_t ev;
+    FRG_CUDA(ctx, cudaEventCreate(&ev));
+    v.push_back(ev);
+  }
+  return FRG_OK;
+}
+
 // gamma of task k: the configured constant (frg.cu:41) or e^{i phi}, phi uniform,
 // drawn from a stream of `seed` reserved for gammas.
 static void task_gammas(const frg_config& c, uint64_t seed, int ntasks, std::vector<cx<double>>& g) {
@@ -206,10 +251,12 @@ static void task_gammas(const frg_config& c, uint64_t seed, int ntasks, std::vec
   }
 }
 
-// Shared body of frg_track / frg_track_async. Device pointers only here.
-static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntasks, const int64_t* ppt,
+// One round on a slot: gammas, start values, then the tracking launches, all on `st`.
+// `evs` (2 * mixed rounds + 1 events, mixed precision only) bracket the FP32 and FP64
+// launches. Device pointers only here.
+static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm, int ntasks, const int64_t* ppt,
                                 uint64_t seed, cx<double>* d_roots, int32_t* d_codes, cx<double>* d_yfinal,
-                                double* d_resid, int64_t N, cudaStream_t st) {
+                                double* d_resid, int64_t N, cudaStream_t st, cudaEvent_t* evs) {
   const bool mixed = ctx->cfg.precision == FRG_PREC_MIXED;
   std::vector<cx<double>> g;
   task_gammas(ctx->cfg, seed, ntasks, g);
@@ -221,51 +268,51 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   }
   std::vector<int64_t> starts(ntasks + 1, 0);
   for (int k = 0; k < ntasks; ++k) starts[k + 1] = starts[k] + ppt[k];
-  FRG_CUDA(ctx, ctx->gamma.ensure(sizeof(cx<double>) * ntasks));
-  FRG_CUDA(ctx, ctx->gamma_lo.ensure(sizeof(cx<float>) * ntasks));
-  FRG_CUDA(ctx, ctx->fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
-  FRG_CUDA(ctx, ctx->fpm_df.ensure(sizeof(cx<df>) * FRG_NP * ntasks));
-  FRG_CUDA(ctx, ctx->gamma_df.ensure(sizeof(cx<df>) * ntasks));
-  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_df.p, g_df.data(), sizeof(cx<df>) * ntasks, cudaMemcpyHostToDevice, st));
-  FRG_CUDA(ctx, ctx->task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
-  FRG_CUDA(ctx, ctx->queue.ensure(sizeof(unsigned long long) * 8));
-  FRG_CUDA(ctx, ctx->counters.ensure(sizeof(unsigned long long) * 40));
-  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma.p, g.data(), sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st));
-  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->gamma_lo.p, g_lo.data(), sizeof(cx<float>) * ntasks, cudaMemcpyHostToDevice,
-                                st));
-  FRG_CUDA(ctx, cudaMemcpyAsync(ctx->task_start.p, starts.data(), sizeof(int64_t) * (ntasks + 1),
+  FRG_CUDA(ctx, sl.gamma.ensure(sizeof(cx<double>) * ntasks));
+  FRG_CUDA(ctx, sl.gamma_lo.ensure(sizeof(cx<float>) * ntasks));
+  FRG_CUDA(ctx, sl.fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, sl.fpm_df.ensure(sizeof(cx<df>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, sl.gamma_df.ensure(sizeof(cx<df>) * ntasks));
+  FRG_CUDA(ctx, sl.task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
+  FRG_CUDA(ctx, sl.queue.ensure(sizeof(unsigned long long) * 8));
+  FRG_CUDA(ctx, sl.counters.ensure(sizeof(unsigned long long) * FRG_NCOUNTERS));
+  // (host-to-device copies from pageable memory are staged before these calls return)
+  FRG_CUDA(ctx, cudaMemcpyAsync(sl.gamma_df.p, g_df.data(), sizeof(cx<df>) * ntasks, cudaMemcpyHostToDevice, st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(sl.gamma.p, g.data(), sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(sl.gamma_lo.p, g_lo.data(), sizeof(cx<float>) * ntasks, cudaMemcpyHostToDevice, st));
+  FRG_CUDA(ctx, cudaMemcpyAsync(sl.task_start.p, starts.data(), sizeof(int64_t) * (ntasks + 1),
                                 cudaMemcpyHostToDevice, st));
-  FRG_CUDA(ctx, cudaMemsetAsync(ctx->queue.p, 0, sizeof(unsigned long long) * 8, st));
-  FRG_CUDA(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * 40, st));
-  FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)ctx->fpm_lo.p, FRG_NP * ntasks, st));
-  FRG_CUDA(ctx, frg_launch_to_df(d_fpm, (cx<df>*)ctx->fpm_df.p, FRG_NP * ntasks, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(sl.queue.p, 0, sizeof(unsigned long long) * 8, st));
+  FRG_CUDA(ctx, cudaMemsetAsync(sl.counters.p, 0, sizeof(unsigned long long) * FRG_NCOUNTERS, st));
+  FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)sl.fpm_lo.p, FRG_NP * ntasks, st));
+  FRG_CUDA(ctx, frg_launch_to_df(d_fpm, (cx<df>*)sl.fpm_df.p, FRG_NP * ntasks, st));
 
   frg::TrackArgs a;
   std::memset(&a, 0, sizeof(a));
   a.cfg = ctx->cfg;
   a.fpm = d_fpm;
-  a.gamma = (const cx<double>*)ctx->gamma.p;
-  a.fpm_lo = (const cx<float>*)ctx->fpm_lo.p;
-  a.gamma_lo = (const cx<float>*)ctx->gamma_lo.p;
-  a.fpm_df = (const cx<df>*)ctx->fpm_df.p;
-  a.gamma_df = (const cx<df>*)ctx->gamma_df.p;
-  a.task_start = (const int64_t*)ctx->task_start.p;
+  a.gamma = (const cx<double>*)sl.gamma.p;
+  a.fpm_lo = (const cx<float>*)sl.fpm_lo.p;
+  a.gamma_lo = (const cx<float>*)sl.gamma_lo.p;
+  a.fpm_df = (const cx<df>*)sl.fpm_df.p;
+  a.gamma_df = (const cx<df>*)sl.gamma_df.p;
+  a.task_start = (const int64_t*)sl.task_start.p;
   a.ntasks = ntasks;
   a.npaths = N;
   a.seed = seed;
-  unsigned long long* q = (unsigned long long*)ctx->queue.p;
+  unsigned long long* q = (unsigned long long*)sl.queue.p;
   a.queue = q;
   a.roots = d_roots;
   a.codes = d_codes;
   a.yfinal = d_yfinal;
   a.resid = d_resid;
   a.work = nullptr;
-  a.counters = (unsigned long long*)ctx->counters.p;
+  a.counters = (unsigned long long*)sl.counters.p;
   const bool team = ctx->cfg.kernel_variant == FRG_KERNEL_TEAM;
   if (team) {  // start values for every path, generated once up front
-    FRG_CUDA(ctx, ctx->starts.ensure(sizeof(cx<double>) * frg::FRG_START_STRIDE * (size_t)N));
-    a.starts = (const cx<double>*)ctx->starts.p;
-    cudaError_t e = frg_launch_starts(a, (cx<double>*)ctx->starts.p, st);
+    FRG_CUDA(ctx, sl.starts.ensure(sizeof(cx<double>) * frg::FRG_START_STRIDE * (size_t)N));
+    a.starts = (const cx<double>*)sl.starts.p;
+    cudaError_t e = frg_launch_starts(a, (cx<double>*)sl.starts.p, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "start kernel launch");
   }
   // persistent grids: SMs x resident blocks, capped by the work (one path per thread
@@ -291,22 +338,15 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
   // conditioned again (and before t_switch) back to the next round's FP32 kernel; the
   // last round keeps every path in FP64 until it ends. Queue heads and counts live in
   // q: [0] FP32 queue, [1] FP64 queue, [2] FP64 list count, [3], [4] hand-back counts.
-  FRG_CUDA(ctx, ctx->handoff.ensure(sizeof(frg::Handoff) * (size_t)N));
-  FRG_CUDA(ctx, ctx->handoff_list.ensure(sizeof(int64_t) * (size_t)N));
-  FRG_CUDA(ctx, ctx->lo_lists.ensure(sizeof(int64_t) * 2 * (size_t)N));
-  a.handoff = (frg::Handoff*)ctx->handoff.p;
-  a.handoff_list = (int64_t*)ctx->handoff_list.p;
+  FRG_CUDA(ctx, sl.handoff.ensure(sizeof(frg::Handoff) * (size_t)N));
+  FRG_CUDA(ctx, sl.handoff_list.ensure(sizeof(int64_t) * (size_t)N));
+  FRG_CUDA(ctx, sl.lo_lists.ensure(sizeof(int64_t) * 2 * (size_t)N));
+  a.handoff = (frg::Handoff*)sl.handoff.p;
+  a.handoff_list = (int64_t*)sl.handoff_list.p;
   a.handoff_count = q + 2;
-  int64_t* lo = (int64_t*)ctx->lo_lists.p;
-  const int rounds = team ? (ctx->cfg.mixed_rounds > 0 ? ctx->cfg.mixed_rounds : 1) : 1;
-  if ((int)ctx->round_ev.size() < 2 * rounds + 1) {
-    while ((int)ctx->round_ev.size() < 2 * rounds + 1) {
-      cudaEvent_t ev;
-      FRG_CUDA(ctx, cudaEventCreate(&ev));
-      ctx->round_ev.push_back(ev);
-    }
-  }
-  FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[0], st));
+  int64_t* lo = (int64_t*)sl.lo_lists.p;
+  const int rounds = mixed_rounds_of(ctx->cfg);
+  FRG_CUDA(ctx, cudaEventRecord(evs[0], st));
   for (int r = 0; r < rounds; ++r) {
     if (r > 0) FRG_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned long long) * 3, st));
     FRG_CUDA(ctx, cudaMemsetAsync(q + 3 + (r & 1), 0, sizeof(unsigned long long), st));
@@ -315,9 +355,10 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
     a.lo_count = r == 0 ? nullptr : q + 3 + ((r - 1) & 1);
     a.back_list = nullptr;
     a.back_count = nullptr;
-    cudaError_t e = launch(1, grid_for(1, N));
+    const int lo_mode = (team && ctx->cfg.lo_points == 1) ? 3 : 1;
+    cudaError_t e = launch(lo_mode, grid_for(lo_mode, N));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
-    FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[2 * r + 1], st));
+    FRG_CUDA(ctx, cudaEventRecord(evs[2 * r + 1], st));
     a.queue = q + 1;
     a.lo_list = nullptr;
     a.lo_count = nullptr;
@@ -325,9 +366,8 @@ static frg_status enqueue_track(frg_ctx* ctx, const cx<double>* d_fpm, int ntask
     a.back_count = q + 3 + (r & 1);
     e = launch(2, grid_for(2, N));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
-    FRG_CUDA(ctx, cudaEventRecord(ctx->round_ev[2 * r + 2], st));
+    FRG_CUDA(ctx, cudaEventRecord(evs[2 * r + 2], st));
   }
-  ctx->last_rounds = rounds;
   return FRG_OK;
 }
 
@@ -356,8 +396,44 @@ extern "C" frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntask
   if (!is_device_ptr(fpm) || !is_device_ptr(roots) || !is_device_ptr(codes) || (yfinal && !is_device_ptr(yfinal)) ||
       (resid && !is_device_ptr(resid)))
     return fail(ctx, FRG_ERR_ARG, "frg_track_async takes device pointers only");
-  return enqueue_track(ctx, (const cx<double>*)fpm, ntasks, paths_per_task, seed, (cx<double>*)roots, codes,
-                       (cx<double>*)yfinal, resid, N, (cudaStream_t)stream);
+  s = ensure_events(ctx, ctx->round_ev, 2 * mixed_rounds_of(ctx->cfg) + 1);
+  if (s != FRG_OK) return s;
+  ctx->last_rounds = 0;  // stage times are not reported for asynchronous calls
+  return enqueue_track(ctx, *ctx->slots[0], (const cx<double>*)fpm, ntasks, paths_per_task, seed,
+                       (cx<double>*)roots, codes, (cx<double>*)yfinal, resid, N, (cudaStream_t)stream,
+                       ctx->round_ev.data());
+}
+
+// Adds one round's counters to stats (stats->paths and times are set by the caller).
+static void add_counters(frg_stats* st, const unsigned long long* cnt, bool mixed) {
+  for (int k = 0; k < 8; ++k) st->codes[k] += (int64_t)cnt[k];
+  st->ivp_solves += (int64_t)cnt[8];
+  st->newton_iters += (int64_t)cnt[9];
+  st->steps += (int64_t)cnt[10];
+  st->fp64_solves += (int64_t)cnt[11];
+  st->handoffs += (int64_t)cnt[12];
+  for (int r = 0; r < 6; ++r) st->handoff_reason[r] += (int64_t)cnt[16 + r];
+  for (int r = 0; r < 12; ++r) st->kernel_cycles[r] += (int64_t)cnt[24 + r];
+  if (mixed) {
+    st->handbacks += (int64_t)cnt[13];
+    for (int b = 0; b < 6; ++b) st->fp64_segment_hist[b] += (int64_t)cnt[40 + b];
+    if ((int64_t)cnt[46] > st->fp64_segment_max) st->fp64_segment_max = (int64_t)cnt[46];
+    st->refine_solves += (int64_t)cnt[22];
+    st->refine_warp_steps += (int64_t)cnt[23];
+  }
+}
+
+// FP32-stage and FP64-stage times of one call-round from its launch events.
+static void stage_times(const cudaEvent_t* evs, int rounds, float* m32, float* m64, double* per_round) {
+  *m32 = *m64 = 0.f;
+  for (int r = 0; r < rounds; ++r) {
+    float m0 = 0.f, m1 = 0.f;
+    cudaEventElapsedTime(&m0, evs[2 * r], evs[2 * r + 1]);
+    cudaEventElapsedTime(&m1, evs[2 * r + 1], evs[2 * r + 2]);
+    *m32 += m0;
+    *m64 += m1;
+    if (per_round && r < 16) { per_round[2 * r] = m0; per_round[2 * r + 1] = m1; }
+  }
 }
 
 extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
@@ -371,6 +447,11 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
   if (N == 0) return FRG_OK;
   FRG_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
+  Slot& sl = *ctx->slots[0];
+  const bool mixed = ctx->cfg.precision == FRG_PREC_MIXED;
+  const int mr = mixed_rounds_of(ctx->cfg);
+  s = ensure_events(ctx, ctx->round_ev, 2 * mr + 1);
+  if (s != FRG_OK) return s;
 
   // inputs
   const cx<double>* d_fpm = (const cx<double>*)fpm;
@@ -395,43 +476,140 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
     }
   }
   FRG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-  s = enqueue_track(ctx, d_fpm, ntasks, paths_per_task, seed, (cx<double>*)outs[0].dev, (int32_t*)outs[1].dev,
-                    (cx<double>*)outs[2].dev, (double*)outs[3].dev, N, st);
+  s = enqueue_track(ctx, sl, d_fpm, ntasks, paths_per_task, seed, (cx<double>*)outs[0].dev, (int32_t*)outs[1].dev,
+                    (cx<double>*)outs[2].dev, (double*)outs[3].dev, N, st, ctx->round_ev.data());
   if (s != FRG_OK) return s;
+  ctx->last_rounds = mixed ? mr : 0;
   FRG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   for (Out& o : outs)
     if (o.user && o.host) FRG_CUDA(ctx, cudaMemcpyAsync(o.user, o.dev, o.bytes, cudaMemcpyDeviceToHost, st));
-  unsigned long long cnt[40], qv[4];
-  FRG_CUDA(ctx, cudaMemcpyAsync(cnt, ctx->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
-  FRG_CUDA(ctx, cudaMemcpyAsync(qv, ctx->queue.p, sizeof(qv), cudaMemcpyDeviceToHost, st));
+  unsigned long long cnt[FRG_NCOUNTERS];
+  FRG_CUDA(ctx, cudaMemcpyAsync(cnt, sl.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
   FRG_CUDA(ctx, cudaStreamSynchronize(st));
   if (stats) {
-    for (int k = 0; k < 8; ++k) stats->codes[k] = (int64_t)cnt[k];
-    stats->ivp_solves = (int64_t)cnt[8];
-    stats->newton_iters = (int64_t)cnt[9];
-    stats->steps = (int64_t)cnt[10];
-    stats->fp64_solves = (int64_t)cnt[11];
-    stats->handoffs = (int64_t)cnt[12];
-    for (int r = 0; r < 6; ++r) stats->handoff_reason[r] = (int64_t)cnt[16 + r];
-    for (int r = 0; r < 12; ++r) stats->kernel_cycles[r] = (int64_t)cnt[24 + r];
-    (void)qv;
+    add_counters(stats, cnt, mixed);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->track_ms = ms;
-    if (ctx->cfg.precision == FRG_PREC_MIXED) {
-      for (int r = 0; r < ctx->last_rounds; ++r) {
-        float m0 = 0.f, m1 = 0.f;
-        cudaEventElapsedTime(&m0, ctx->round_ev[2 * r], ctx->round_ev[2 * r + 1]);
-        cudaEventElapsedTime(&m1, ctx->round_ev[2 * r + 1], ctx->round_ev[2 * r + 2]);
-        stats->stage_ms[0] += m0;
-        stats->stage_ms[1] += m1;
-      }
-      stats->handbacks = (int64_t)cnt[13];
-      stats->refine_solves = (int64_t)cnt[22];
-      stats->refine_warp_steps = (int64_t)cnt[23];
+    if (mixed) {
+      float m32, m64;
+      stage_times(ctx->round_ev.data(), mr, &m32, &m64, stats->round_ms);
+      stats->stage_ms[0] = m32;
+      stats->stage_ms[1] = m64;
     } else {
       stats->stage_ms[1] = ms;
     }
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return FRG_OK;
+}
+
+extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                                       int nrounds, const uint64_t* seeds, int depth, double* roots, int32_t* codes,
+                                       double* resid, frg_stats* stats) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (!ctx) return FRG_ERR_ARG;
+  if (nrounds < 1 || !seeds) return fail(ctx, FRG_ERR_ARG, "need nrounds >= 1 and one seed per round");
+  if (depth < 1 || depth > 8) return fail(ctx, FRG_ERR_ARG, "depth must be in 1..8");
+  int64_t N = 0;
+  frg_status s = check_track_args(ctx, fpm, ntasks, paths_per_task, roots, codes, &N);
+  if (s != FRG_OK) return s;
+  if (stats) { std::memset(stats, 0, sizeof(*stats)); stats->paths = N * nrounds; }
+  if (N == 0) return FRG_OK;
+  FRG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const bool mixed = ctx->cfg.precision == FRG_PREC_MIXED;
+  const int mr = mixed_rounds_of(ctx->cfg);
+  if (depth > nrounds) depth = nrounds;
+  while ((int)ctx->slots.size() < depth) {
+    Slot* sl = new (std::nothrow) Slot();
+    if (!sl) return fail(ctx, FRG_ERR_ALLOC, "slot allocation");
+    cudaError_t e = cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete sl; return cuda_fail(ctx, e, "cudaStreamCreateWithFlags"); }
+    sl->own_stream = true;
+    ctx->slots.push_back(sl);
+  }
+  // the task parameters, once, before any round
+  const cx<double>* d_fpm = (const cx<double>*)fpm;
+  if (!is_device_ptr(fpm)) {
+    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks));
+    FRG_CUDA(ctx, cudaMemcpy(ctx->fpm.p, fpm, sizeof(cx<double>) * 30 * ntasks, cudaMemcpyHostToDevice));
+    d_fpm = (const cx<double>*)ctx->fpm.p;
+  }
+  const bool dev_out = is_device_ptr(roots);
+  if (is_device_ptr(codes) != dev_out || (resid && is_device_ptr(resid) != dev_out))
+    return fail(ctx, FRG_ERR_ARG, "roots, codes and resid must all be device or all be host buffers");
+  // pinned copies of every round's counters
+  const size_t ncnt = (size_t)nrounds * FRG_NCOUNTERS;
+  if (ctx->h_counters_n < ncnt) {
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    ctx->h_counters = nullptr;
+    ctx->h_counters_n = 0;
+    FRG_CUDA(ctx, cudaHostAlloc((void**)&ctx->h_counters, sizeof(unsigned long long) * ncnt, cudaHostAllocDefault));
+    ctx->h_counters_n = ncnt;
+  }
+  // events: start, per round its launch events and its end
+  const int per = 2 * mr + 1;
+  std::vector<cudaEvent_t> evs;
+  s = ensure_events(ctx, evs, (size_t)nrounds * (per + 1) + 1);
+  if (s != FRG_OK) return s;
+  struct EvGuard {
+    std::vector<cudaEvent_t>& v;
+    ~EvGuard() { for (cudaEvent_t e : v) cudaEventDestroy(e); }
+  } guard{evs};
+  cudaEvent_t ev_start = evs.back();
+  FRG_CUDA(ctx, cudaEventRecord(ev_start, ctx->slots[0]->stream));
+  for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, ev_start, 0));
+  const size_t rb = sizeof(cx<double>) * 21 * (size_t)N, cb = sizeof(int32_t) * (size_t)N,
+               eb = sizeof(double) * (size_t)N;
+  for (int r = 0; r < nrounds; ++r) {
+    Slot& sl = *ctx->slots[r % depth];
+    cudaStream_t st = sl.stream;
+    cx<double>* d_roots;
+    int32_t* d_codes;
+    double* d_resid = nullptr;
+    if (dev_out) {
+      d_roots = (cx<double>*)((char*)roots + rb * r);
+      d_codes = (int32_t*)((char*)codes + cb * r);
+      if (resid) d_resid = (double*)((char*)resid + eb * r);
+    } else {
+      FRG_CUDA(ctx, sl.roots.ensure(rb));
+      FRG_CUDA(ctx, sl.codes.ensure(cb));
+      d_roots = (cx<double>*)sl.roots.p;
+      d_codes = (int32_t*)sl.codes.p;
+      if (resid) { FRG_CUDA(ctx, sl.resid.ensure(eb)); d_resid = (double*)sl.resid.p; }
+    }
+    cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
+    s = enqueue_track(ctx, sl, d_fpm, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
+                      rev);
+    if (s != FRG_OK) return s;
+    FRG_CUDA(ctx, cudaEventRecord(rev[per], st));
+    if (!dev_out) {  // host outputs: asynchronous when the caller's buffers are pinned
+      FRG_CUDA(ctx, cudaMemcpyAsync((char*)roots + rb * r, d_roots, rb, cudaMemcpyDeviceToHost, st));
+      FRG_CUDA(ctx, cudaMemcpyAsync((char*)codes + cb * r, d_codes, cb, cudaMemcpyDeviceToHost, st));
+      if (resid) FRG_CUDA(ctx, cudaMemcpyAsync((char*)resid + eb * r, d_resid, eb, cudaMemcpyDeviceToHost, st));
+    }
+    FRG_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters + (size_t)r * FRG_NCOUNTERS, sl.counters.p,
+                                  sizeof(unsigned long long) * FRG_NCOUNTERS, cudaMemcpyDeviceToHost, st));
+  }
+  for (int d = 0; d < depth; ++d) FRG_CUDA(ctx, cudaStreamSynchronize(ctx->slots[d]->stream));
+  if (stats) {
+    float span = 0.f;
+    for (int r = 0; r < nrounds; ++r) {
+      add_counters(stats, ctx->h_counters + (size_t)r * FRG_NCOUNTERS, mixed);
+      cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
+      float end = 0.f;
+      cudaEventElapsedTime(&end, ev_start, rev[per]);
+      if (end > span) span = end;
+      if (mixed) {
+        float m32, m64;
+        stage_times(rev, mr, &m32, &m64, nullptr);
+        stats->stage_ms[0] += m32;
+        stats->stage_ms[1] += m64;
+        if (r < 16) { stats->round_ms[2 * r] = m32; stats->round_ms[2 * r + 1] = m64; }
+      }
+    }
+    stats->track_ms = span;
+    if (!mixed) stats->stage_ms[1] = span;
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return FRG_OK;

@@ -1,9 +1,9 @@
 // Complex arithmetic for the tracker kernels, templated on the real type so the
 // same code runs in FP64 (the reference's precision, classes.cuh:24-36) and FP32.
 //
-// Multiplication is the textbook formula with fused multiply-adds; division is
+// Multiplication is the textbook formula with fused multiply-adds; FP32 division is
 // Smith's algorithm (R. L. Smith, "Algorithm 116: Complex division", CACM 5(8),
-// 1962), which avoids the overflow of the naive |b|^2 form.
+// 1962), which avoids the overflow of the naive |b|^2 form in FP32's narrow range.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -82,3 +82,13 @@ FRG_HD cx<T> cinv(cx<T> b) {
     return cx<T>(r * id, -id);
   }
 }
+
+// FP64: 1/b = conj(b) / |b|^2 with one reciprocal. The tracker's FP64 operands are
+// far inside the range where |b|^2 neither overflows nor underflows, so Smith's
+// scaling (two divisions) buys nothing there; FP32 keeps Smith's form.
+FRG_HD cx<double> cinv(cx<double> b) {
+  const double r = 1.0 / (b.re * b.re + b.im * b.im);
+  return cx<double>(b.re * r, -b.im * r);
+}
+FRG_HD cx<double> cdiv(cx<double> a, cx<double> b) { return a * cinv(b); }
+

@@ -32,6 +32,10 @@ struct Handoff {
 
 // Device-side arguments of one tracking launch. All arrays are device memory.
 constexpr int FRG_START_STRIDE = 51;
+// counters: codes[8], ivp, newton, steps, fp64 solves, handoffs, hand-backs, -, -, handoff
+// reasons 1..6 at [16..21], refinement solves and warp steps at [22..23], kernel cycles at
+// [24..35], -, FP64-segment histogram at [40..45], longest FP64 segment at [46]
+#define FRG_NCOUNTERS 48
 
 struct TrackArgs {
   frg_config cfg;
@@ -51,8 +55,7 @@ struct TrackArgs {
   cx<double>* yfinal;           // npaths x 23, optional
   double* resid;                // npaths, optional
   int32_t* work;                // npaths x 3 (ivp solves, newton iterations, steps), optional
-  unsigned long long* counters; // 40: codes[8], ivp, newton, steps, fp64 solves, handoffs, hand-backs, -,
-                                //     handoff reasons 1..6 at [16..21], kernel cycles at [24..35]
+  unsigned long long* counters; // FRG_NCOUNTERS counters (layout above)
   const cx<double>* starts;     // npaths x FRG_START_STRIDE start values (null: generated inline)
   Handoff* handoff;             // npaths slots (mixed precision)
   int64_t* handoff_list;        // ids of paths handed to the FP64 kernel

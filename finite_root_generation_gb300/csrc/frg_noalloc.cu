@@ -34,7 +34,7 @@ namespace {
 
 struct NoallocScratch {
   unsigned long long queue[4];
-  unsigned long long counters[40];
+  unsigned long long counters[FRG_NCOUNTERS];
   cx<double> gamma[FRG_NOALLOC_MAX_TASKS];
   int64_t task_start[FRG_NOALLOC_MAX_TASKS + 1];
 };

@@ -29,10 +29,10 @@
 namespace frg {
 namespace team {
 
-// Type of the path's points (Yc, Yn, YN) and of the refinement residual: FP64 in the
-// FP64 kernels, double-float in the FP32 stage.
+// Type of the path's points (Yc, Yn, YN) and of the FP32 stage's refinement residual:
+// FP64 by default; the FP32 stage can instead keep them in double-float (P = df), which
+// runs on the FP32 pipes but is ~10x more code than the FP64 form.
 template <typename T> struct PointOf { typedef double type; };
-template <> struct PointOf<float> { typedef df type; };
 
 constexpr int TEAM = 8;
 constexpr int NG = 16;  // links (14), Z0, t
@@ -85,9 +85,8 @@ __device__ __forceinline__ T team_min(unsigned mask, T v) {
 // upper factor for the back substitution. The 32-byte pad makes the stride between
 // teams 32 bytes past a multiple of 128, so the four teams of a warp reading "the
 // same" field hit different bank groups.
-template <typename T>
+template <typename T, typename P = typename PointOf<T>::type>
 struct Smem {
-  typedef typename PointOf<T>::type P;
   cx<P> Yc[VS], Yn[VS], YN[VS];
   cx<P> spm[32];
   cx<T> Vc[VS], Vn[VS], u[VS], Ye[VS], dx[VS];
@@ -148,8 +147,8 @@ __device__ __forceinline__ void residual_hi(const cx<P>* Yd, const cx<P>* spm, c
 // One step of the dense phase over a window of W columns: the current pivot column
 // is index 0; rows shift one column left as they are eliminated, so a rolled loop
 // needs no dynamic register indexing. The pivot row (final once chosen) goes to S.U.
-template <typename T, int W>
-__device__ __forceinline__ void lu_window_step(Smem<T>& S, int k, int g, cx<T>* R0, cx<T>& R0r, cx<T>* R1,
+template <typename T, int W, typename P>
+__device__ __forceinline__ void lu_window_step(Smem<T, P>& S, int k, int g, cx<T>* R0, cx<T>& R0r, cx<T>* R1,
                                                cx<T>& R1r, bool& used0, bool& used1, T& pmax, T& pmin) {
   const unsigned FULL = 0xffffffffu;
   const cx<T> zero(T(0));
@@ -202,17 +201,15 @@ __device__ __forceinline__ void lu_window_step(Smem<T>& S, int k, int g, cx<T>* 
 //     H at the FP64 point S.YN; when T is float, H is evaluated in FP64 if `hires`
 //     and in FP32 (at the rounded point) otherwise.
 // The solution is written to dst[0..22] (shared memory).
-template <typename T>
-__device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc, cx<T>* dst, bool newton,
+template <typename T, typename P>
+__device__ __forceinline__ StepOut<T> linear_step(Smem<T, P>& S, const cx<T>* Wsrc, cx<T>* dst, bool newton,
                                                   bool tstep, T tgoal, const LaneParams<T>& lp,
-                                                  const cx<typename PointOf<T>::type>* fpm_hi,
-                                                  cx<typename PointOf<T>::type> gamma_hi, int g, bool hires) {
-  typedef typename PointOf<T>::type P;
+                                                  const cx<P>* fpm_hi, cx<P> gamma_hi, int g, bool hires) {
   const unsigned FULL = 0xffffffffu;
   const bool grp = g < 7;
   const int j = grp ? g + 1 : 7;
   const cx<T> zero(T(0));
-  constexpr bool LOWP = sizeof(T) < sizeof(double);
+  constexpr bool LOWP = sizeof(T) < sizeof(P);
   // `newton` and `hires` are per team, so reductions inside branches on them use the
   // team's own mask; everything outside such branches runs on the full warp
   const unsigned tmask = 0xffu << (threadIdx.x & 24);
@@ -371,13 +368,13 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T>& S, const cx<T>* Wsrc,
   bool used0 = false, used1 = false;
   T pmax = T(0), pmin = T(3.0e38);
 #pragma unroll 1
-  for (int k = 0; k < 8; ++k) lu_window_step<T, 16>(S, k, g, R0, R0r, R1, R1r, used0, used1, pmax, pmin);
+  for (int k = 0; k < 8; ++k) lu_window_step<T, 16, P>(S, k, g, R0, R0r, R1, R1r, used0, used1, pmax, pmin);
   {
     cx<T> Q0[8], Q1[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) { Q0[c] = R0[c]; Q1[c] = R1[c]; }
 #pragma unroll 1
-    for (int k = 8; k < 16; ++k) lu_window_step<T, 8>(S, k, g, Q0, R0r, Q1, R1r, used0, used1, pmax, pmin);
+    for (int k = 8; k < 16; ++k) lu_window_step<T, 8, P>(S, k, g, Q0, R0r, Q1, R1r, used0, used1, pmax, pmin);
   }
   __syncwarp();
   // ---- back substitution, column by column; lane g keeps the right-hand sides of

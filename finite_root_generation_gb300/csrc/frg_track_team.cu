@@ -183,7 +183,7 @@ __device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, i
   __syncwarp(tmask);
 }
 
-template <int MODE, typename T>
+template <int MODE, typename T, typename P = typename PointOf<T>::type>
 __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr bool LO = (MODE == MODE_LO);
@@ -192,12 +192,11 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   const int lane = threadIdx.x & 31;
   const int g = lane & 7;
   const unsigned tmask = 0xffu << (lane & 24);
-  typedef typename PointOf<T>::type P;
   typedef cx<P> cp;
-  Smem<T>& S = reinterpret_cast<Smem<T>*>(smem_raw)[threadIdx.x >> 3];
+  Smem<T, P>& S = reinterpret_cast<Smem<T, P>*>(smem_raw)[threadIdx.x >> 3];
   {
     cx<T>* base = reinterpret_cast<cx<T>*>(&S);
-    for (int i = g; i < (int)(sizeof(Smem<T>) / sizeof(cx<T>)); i += TEAM) base[i] = cx<T>(T(0));
+    for (int i = g; i < (int)(sizeof(Smem<T, P>) / sizeof(cx<T>)); i += TEAM) base[i] = cx<T>(T(0));
   }
   // The FP32 stage's corrector iterates on FP32 residuals until |dY| falls below
   // newt_tol_lo (or stops shrinking), then on FP64 residuals to the reference's
@@ -355,7 +354,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     long long tc2 = clock64();
 
     // ========================================== linear step (whole warp)
-    const StepOut<T> r = linear_step<T>(S, Wsrc, dst, newton, tstep, tgoal, lp, fpm_hi_of<P>(a, task),
+    const StepOut<T> r = linear_step<T, P>(S, Wsrc, dst, newton, tstep, tgoal, lp, fpm_hi_of<P>(a, task),
                                         gamma_hi_of<P>(a, task), g, hires);
     __syncwarp();
     long long tc3 = clock64();
@@ -443,7 +442,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       const int max_its = sharp ? c.sharp_its : c.newt_its;
       const T tol = sharp ? T(c.sharp_tol) : newt_tol;
       const int restype = (LO || sharp) ? (LO ? 1 : c.sharp_residual) : c.newt_residual;
-      bool done = false;
+      bool done = false, predicted = false;
       if (restype == 0 && it > 0) {
         residual = r.hnorm;  // |H| at the current point: the residual of the previous update
         if (!(it < max_its && residual > tol)) done = true;
@@ -461,14 +460,22 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
             if ((floor_ && !c.lo_refine) || !(it < max_its)) done = true;
           } else if (!(it < max_its && residual > tol)) {
             done = true;
+          } else if (LO && !sharp && c.lo_refine == 2 &&
+                     residual * (r.ratio * T(1e-6) + residual * T(100)) < T(0.1) * tol) {
+            // refined iteration whose successor is predicted below the tolerance: the
+            // FP32 solve contracts the error by about cond * 2^-24 (ratio * 1e-6 with a
+            // safety factor of 16) on top of Newton's quadratic term
+            done = true;
+            predicted = true;
           }
           res_prev = residual;
         }
       }
       __syncwarp(tmask);
       if (done) {
-        const bool ok = (LO && !c.lo_refine && !sharp) ? residual < T(c.newt_tol_lo) * T(100)
-                                                        : (hires || !LO) && residual < (sharp ? T(c.sharp_tol) : newt_tol);
+        const bool ok = predicted || ((LO && !c.lo_refine && !sharp)
+                                          ? residual < T(c.newt_tol_lo) * T(100)
+                                          : (hires || !LO) && residual < (sharp ? T(c.sharp_tol) : newt_tol));
         if (ministep++ == c.max_ministeps) { code = 2; finished = true; final_from_YN = sharp; }
         else if (ok && !sharp) {
           if (fabs(1.0 - double(S.Yn[22].re)) < c.sharp_trigger) {
@@ -540,6 +547,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     __syncwarp(tmask);
     if (lane == 0) cyc[3] += clock64() - tc3;
 
+    if (MODE == MODE_RESUME && (finished || handback) && g == 0 && a.counters) {
+      // length of this path's FP64 segment in this launch
+      const int b = seg < 100 ? 0 : seg < 300 ? 1 : seg < 1000 ? 2 : seg < 3000 ? 3 : seg < 10000 ? 4 : 5;
+      atomicAdd(&a.counters[40 + b], 1ull);
+      atomicMax(&a.counters[46], (unsigned long long)seg);
+    }
     if ((LO && (handoff || finished)) || handback) {
       // save the state for the other precision's kernel (an FP32 path is always
       // finished in FP64; an FP64 path well conditioned again returns to FP32)
@@ -623,22 +636,23 @@ cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cu
 }
 
 namespace {
-template <int MODE, typename T>
+template <int MODE, typename T, typename P = typename frg::team::PointOf<T>::type>
 cudaError_t team_launch(const frg::TrackArgs& args, int grid, cudaStream_t stream) {
-  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T>);
-  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T, P>);
+  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T, P>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  frg::team::team_kernel<MODE, T><<<grid, FRG_TEAM_THREADS, smem, stream>>>(args);
+  frg::team::team_kernel<MODE, T, P><<<grid, FRG_TEAM_THREADS, smem, stream>>>(args);
   return cudaGetLastError();
 }
-template <int MODE, typename T>
+template <int MODE, typename T, typename P = typename frg::team::PointOf<T>::type>
 cudaError_t team_occ(int* bps) {
-  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T>);
-  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  const size_t smem = (FRG_TEAM_THREADS / 8) * sizeof(frg::team::Smem<T, P>);
+  cudaError_t e = cudaFuncSetAttribute(frg::team::team_kernel<MODE, T, P>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, frg::team::team_kernel<MODE, T>, FRG_TEAM_THREADS, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, frg::team::team_kernel<MODE, T, P>, FRG_TEAM_THREADS,
+                                                       smem);
 }
 }  // namespace
 
@@ -647,6 +661,7 @@ cudaError_t frg_launch_team(int mode, const frg::TrackArgs& args, int grid, cuda
     case 0: return team_launch<frg::team::MODE_PLAIN, double>(args, grid, stream);
     case 1: return team_launch<frg::team::MODE_LO, float>(args, grid, stream);
     case 2: return team_launch<frg::team::MODE_RESUME, double>(args, grid, stream);
+    case 3: return team_launch<frg::team::MODE_LO, float, df>(args, grid, stream);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -656,6 +671,7 @@ cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm) {
     case 0: return team_occ<frg::team::MODE_PLAIN, double>(blocks_per_sm);
     case 1: return team_occ<frg::team::MODE_LO, float>(blocks_per_sm);
     case 2: return team_occ<frg::team::MODE_RESUME, double>(blocks_per_sm);
+    case 3: return team_occ<frg::team::MODE_LO, float, df>(blocks_per_sm);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -91,13 +91,16 @@ typedef struct frg_config {
   int mixed_rounds;      /* mixed, team kernels: FP32/FP64 rounds; a path well conditioned again in
                             FP64 returns to FP32 in the next round (1 = no return) */
   int lo_refine;         /* mixed: 1 = the FP32 corrector refines on double-float residuals to
-                            newt_tol; 0 = it stops at newt_tol_lo */
+                            newt_tol; 2 = the same, but a refined iteration whose successor is
+                            predicted below newt_tol / 10 ends it; 0 = it stops at newt_tol_lo */
   int lo_endgame;        /* mixed: 1 = the FP32 stage (with refinement) also runs the endgame and
                             sharpening, FP64 only for ill-conditioned steps; 0 = FP64 from t_switch */
   int64_t path_offset;   /* random stream of local path i is path_offset + i: shards of one round
                             (path-index ranges on several GPUs) reproduce the single-GPU round */
   int fp64_budget;       /* mixed: a path that spends more FP64 solves than this in one FP64 launch
                             ends with code 2 (step limit); 0 = no limit */
+  int lo_points;         /* mixed, team kernels: the FP32 stage keeps its points and refinement
+                            residuals in 0 = FP64, 1 = double-float (FP32 pipes, larger code) */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */
@@ -120,6 +123,10 @@ typedef struct frg_stats {
   int64_t handbacks;       /* mixed: returns from FP64 to FP32 once well conditioned again */
   int64_t refine_solves;   /* mixed: FP32-stage corrector iterations on double-float residuals */
   int64_t refine_warp_steps; /* mixed: FP32-stage warp steps in which at least one path refined */
+  double round_ms[32];     /* mixed: FP32-stage and FP64-stage times of rounds 0..15, interleaved */
+  int64_t fp64_segment_hist[6]; /* mixed: paths leaving an FP64 launch after <100, <300, <1000, <3000,
+                                   <10000, >=10000 FP64 solves in it */
+  int64_t fp64_segment_max;     /* mixed: most FP64 solves one path spent in one FP64 launch */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;
@@ -155,6 +162,17 @@ frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t*
 frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
                            uint64_t seed, double* roots, int32_t* codes, double* yfinal, double* resid,
                            void* stream);
+
+/* `nrounds` rounds of the reference driver's loop (frg.cu:351-514, one Homotopy launch
+ * per round, seeds[r] in place of its time(NULL) reseed at :359) in one call, pipelined:
+ * up to `depth` rounds are in flight on separate streams, so a round's long FP64 tail
+ * overlaps the next rounds' tracking. Round r writes roots + r*N*21*2, codes + r*N and
+ * resid + r*N (N = sum of paths_per_task); these are all device or all host buffers
+ * (host copies are asynchronous when the host memory is pinned). stats sums all rounds;
+ * track_ms spans the first launch to the last round's end. */
+frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                            int nrounds, const uint64_t* seeds, int depth, double* roots, int32_t* codes,
+                            double* resid, frg_stats* stats);
 
 /* Plain FP64 tracking that allocates no device memory. No counterpart in the
  * reference: it is for callers that may not call cudaMalloc / cudaFree, such as code
