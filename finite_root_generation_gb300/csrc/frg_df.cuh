@@ -129,26 +129,32 @@ __device__ __forceinline__ df df_rcp(df y) {
   return df(s, t);
 }
 
-__device__ __forceinline__ cx<df> operator+(cx<df> a, cx<df> b) { return cx<df>(a.re + b.re, a.im + b.im); }
-__device__ __forceinline__ cx<df> operator-(cx<df> a, cx<df> b) { return cx<df>(a.re - b.re, a.im - b.im); }
-__device__ __forceinline__ cx<df> operator*(cx<df> a, cx<df> b) {
+// The complex operations are real calls, not inlined: the refinement residual is a
+// straight-line sequence of ~120 of them, and inlining every one makes its code about
+// 77 KB, which evicts the FP32 step from the instruction cache; as calls it is ~30 KB.
+static __device__ __noinline__ cx<df> df_cadd(cx<df> a, cx<df> b) { return cx<df>(a.re + b.re, a.im + b.im); }
+static __device__ __noinline__ cx<df> df_csub(cx<df> a, cx<df> b) { return cx<df>(a.re - b.re, a.im - b.im); }
+static __device__ __noinline__ cx<df> df_cmul(cx<df> a, cx<df> b) {
   return cx<df>(df_dot2(a.re, b.re, a.im, b.im, -1.f), df_dot2(a.re, b.im, a.im, b.re, 1.f));
 }
+__device__ __forceinline__ cx<df> operator+(cx<df> a, cx<df> b) { return df_cadd(a, b); }
+__device__ __forceinline__ cx<df> operator-(cx<df> a, cx<df> b) { return df_csub(a, b); }
+__device__ __forceinline__ cx<df> operator*(cx<df> a, cx<df> b) { return df_cmul(a, b); }
 __device__ __forceinline__ cx<df> operator*(df s, cx<df> a) { return cx<df>(s * a.re, s * a.im); }
 __device__ __forceinline__ cx<df> operator*(cx<df> a, df s) { return cx<df>(s * a.re, s * a.im); }
 __device__ __forceinline__ cx<df>& operator+=(cx<df>& a, cx<df> b) { a = a + b; return a; }
 __device__ __forceinline__ cx<df>& operator-=(cx<df>& a, cx<df> b) { a = a - b; return a; }
 // a - b*c
-__device__ __forceinline__ cx<df> cfms(cx<df> a, cx<df> b, cx<df> c) {
+static __device__ __noinline__ cx<df> cfms(cx<df> a, cx<df> b, cx<df> c) {
   return cx<df>(df_dot2_acc(a.re, -b.re, c.re, b.im, c.im, 1.f), df_dot2_acc(a.im, -b.re, c.im, b.im, c.re, -1.f));
 }
 // a + b*c
-__device__ __forceinline__ cx<df> cfma(cx<df> b, cx<df> c, cx<df> a) {
+static __device__ __noinline__ cx<df> cfma(cx<df> b, cx<df> c, cx<df> a) {
   return cx<df>(df_dot2_acc(a.re, b.re, c.re, b.im, c.im, -1.f), df_dot2_acc(a.im, b.re, c.im, b.im, c.re, 1.f));
 }
 __device__ __forceinline__ df cnorm2(cx<df> a) { return df_dot2(a.re, a.re, a.im, a.im, 1.f); }
 // 1/b = conj(b) / |b|^2 (the tracker's operands are far from the FP32 range limits)
-__device__ __forceinline__ cx<df> cinv(cx<df> b) {
+static __device__ __noinline__ cx<df> cinv(cx<df> b) {
   const df r = df_rcp(cnorm2(b));
   return cx<df>(b.re * r, -(b.im * r));
 }
