@@ -11,11 +11,14 @@ benchmark data; tasks and starts are seeded.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--paths P] [--impl ours|reference]
 
-value    distinct finite roots / second of device tracking time (inputs resident in HBM) of the
-         chosen configuration: mixed precision (FP32 team stage, FP64 endgame and sharpening);
-         plain FP64 on the same seeds gives `plain_fp64`, the speed-up and the recall
-e2e      the same through the public C ABI with host buffers: per step the task upload,
-         tracking, the copy of roots/codes/residuals back and the host duplicate merge
+value    distinct finite roots / second over K rounds (steps) of the chosen configuration run
+         through frg_track_rounds with `--depth` rounds in flight (inputs resident in HBM, CUDA
+         events on the launching streams); the chosen configuration is mixed precision (FP32
+         team kernel with double-float refinement, FP64 for ill-conditioned steps and for
+         finishing every root). Plain FP64 on the same seeds, pipelined the same way, gives
+         `plain_fp64`, the speed-up and the recall
+e2e      the same through the public C ABI with pinned host buffers: the task upload, tracking,
+         the copy of roots/codes/residuals back and the host duplicate merge of every round
 --impl reference  times the reference algorithm's CPU implementation (the C
          restatement in oracle/, the reference's own sources cannot be built on the GPU
          host) on all host cores, on a bounded sample of the same workload.
@@ -212,8 +215,10 @@ def flops_per_solve():
 def _chosen_overrides():
     """The chosen configuration on top of the workload's: mixed precision, the FP32
     stage also running the endgame and sharpening (double-float refinement), FP64 for
-    steps whose condition estimate exceeds 1e5 and for finishing every root."""
-    return dict(mixed_rounds=1, lo_endgame=1, cond_switch=1e5, lo_points=1)
+    steps whose condition estimate exceeds 1e5 and for finishing every root, and at most
+    10,000 FP64 solves per path (a path still going after that ends as a step-limit
+    failure; such paths are crawling near a singularity and set the FP64 tail)."""
+    return dict(mixed_rounds=1, lo_endgame=1, cond_switch=1e5, lo_points=1, fp64_budget=10000)
 
 
 def _round_sets(roots, codes, resid, n, k):
@@ -366,9 +371,10 @@ def run_ours(args, rank, world):
                    "paths_per_step": n, "rounds_in_flight": depth,
                    "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
                              "sharpening included), FP64 team kernel for steps with condition estimate > 1e5 "
-                             "and for finishing",
-                   "l2": "not flushed: per-round state (start values 816 B, hand-off record 1.2 KB, outputs "
-                         "348 B per path: ~155 MB per round, two rounds in flight) exceeds the 129 MB L2",
+                             "(at most 10,000 FP64 solves per path) and for finishing",
+                   "l2": f"not flushed: per-round state (start values 816 B, hand-off record 1.2 KB, outputs "
+                         f"348 B per path: ~{n * 2364 / 1e6:.0f} MB per round, {depth} rounds in flight) exceeds "
+                         "the 129 MB L2",
                    "parallelism": f"replicas x{world}"},
         "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": kp,
                        "ms_per_step": round(p_ms / kp, 3),
@@ -463,7 +469,7 @@ def main():
     ap.add_argument("--paths", type=int, default=65536)
     ap.add_argument("--cpu-sample", type=int, default=8192)
     ap.add_argument("--plain-steps", type=int, default=3)
-    ap.add_argument("--depth", type=int, default=3, help="rounds in flight")
+    ap.add_argument("--depth", type=int, default=4, help="rounds in flight")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

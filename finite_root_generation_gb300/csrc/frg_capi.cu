@@ -129,6 +129,9 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->path_offset = 0;
   c->fp64_budget = 0;
   c->lo_points = 0;
+  c->fp64_segment = 96;
+  c->handback_good = 16;
+  c->lo_final = 0;
   return FRG_OK;
 }
 
@@ -152,6 +155,9 @@ static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->fp64_budget < 0) return fail(ctx, FRG_ERR_ARG, "fp64_budget must be non-negative");
   if (c->lo_refine < 0 || c->lo_refine > 2) return fail(ctx, FRG_ERR_ARG, "lo_refine must be 0, 1 or 2");
   if (c->lo_points < 0 || c->lo_points > 1) return fail(ctx, FRG_ERR_ARG, "lo_points must be 0 or 1");
+  if (c->lo_final < 0 || c->lo_final > 1) return fail(ctx, FRG_ERR_ARG, "lo_final must be 0 or 1");
+  if (c->fp64_segment < 0 || c->handback_good < 0)
+    return fail(ctx, FRG_ERR_ARG, "fp64_segment and handback_good must be non-negative");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   return FRG_OK;
@@ -355,6 +361,7 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
     a.lo_count = r == 0 ? nullptr : q + 3 + ((r - 1) & 1);
     a.back_list = nullptr;
     a.back_count = nullptr;
+    a.lo_keep_ill = (ctx->cfg.lo_final && rounds > 1 && r + 1 == rounds) ? 1 : 0;
     const int lo_mode = (team && ctx->cfg.lo_points == 1) ? 3 : 1;
     cudaError_t e = launch(lo_mode, grid_for(lo_mode, N));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");

@@ -64,6 +64,7 @@ struct TrackArgs {
   const unsigned long long* lo_count;
   int64_t* back_list;           // FP64 kernel: paths handed back to FP32 (null: none, e.g. the last round)
   unsigned long long* back_count;
+  int lo_keep_ill;              // FP32 kernel: 1 = no hand-off for ill-conditioned steps (last round)
 };
 
 }  // namespace frg

@@ -209,12 +209,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   const bool lo_resume = LO && a.lo_list != nullptr;
   const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count
                          : (lo_resume ? (int64_t)*a.lo_count : a.npaths);
-  // A path returns from FP64 to the next round's FP32 kernel after kBackSteps
-  // consecutive well-conditioned solves, or after kSegment FP64 solves in this launch
+  // A path returns from FP64 to the next round's FP32 kernel after handback_good
+  // consecutive well-conditioned solves, or after fp64_segment FP64 solves in this launch
   // (FP64 latency per solve is high on this part, so long FP64 segments set a launch's
   // tail; a path still ill conditioned is simply handed over again by the FP32 kernel).
-  constexpr int kBackSteps = 16;
-  constexpr int kSegment = 96;
+  const int kBackSteps = c.handback_good > 0 ? c.handback_good : 0x7fffffff;
+  const int kSegment = c.fp64_segment > 0 ? c.fp64_segment : 96;
   constexpr int kMaxBounces = 64;
 
   LaneParams<T> lp;
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     int handoff = 0;
     bool handback = false;
     bool final_from_YN = false;
-    if (LO && !(r.ratio <= T(c.cond_switch))) {
+    if (LO && !(r.ratio <= T(c.cond_switch)) && !(a.lo_keep_ill && r.ratio - r.ratio == T(0))) {
       handoff = 2;  // ill-conditioned (or non-finite) step: continue in FP64 from Yc
     } else if (MODE == MODE_RESUME && c.fp64_budget > 0 && seg >= c.fp64_budget) {
       code = 2;  // the FP64 budget of this path is spent: retire it as a step-limit failure

@@ -101,6 +101,13 @@ typedef struct frg_config {
                             ends with code 2 (step limit); 0 = no limit */
   int lo_points;         /* mixed, team kernels: the FP32 stage keeps its points and refinement
                             residuals in 0 = FP64, 1 = double-float (FP32 pipes, larger code) */
+  int fp64_segment;      /* mixed, mixed_rounds >= 2: FP64 solves after which a path returns to the
+                            next round's FP32 kernel at its next accepted step (0 = 96) */
+  int handback_good;     /* mixed, mixed_rounds >= 2: consecutive well-conditioned FP64 solves after
+                            which a path returns to FP32 (0 = only after fp64_segment) */
+  int lo_final;          /* mixed, mixed_rounds >= 2: 1 = the last round's FP32 kernel keeps paths
+                            whose steps are ill conditioned (no hand-off for conditioning); paths
+                            then use FP64 only for one bounded segment per earlier round */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */
