@@ -75,7 +75,7 @@ class FrgStats(ctypes.Structure):
         ("kernel_cycles", ctypes.c_int64 * 12), ("handbacks", ctypes.c_int64),
         ("refine_solves", ctypes.c_int64), ("refine_warp_steps", ctypes.c_int64),
         ("round_ms", ctypes.c_double * 32), ("fp64_segment_hist", ctypes.c_int64 * 6),
-        ("fp64_segment_max", ctypes.c_int64),
+        ("fp64_segment_max", ctypes.c_int64), ("retired", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -86,7 +86,7 @@ class FrgStats(ctypes.Structure):
                 "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks,
                 "refine_solves": self.refine_solves, "refine_warp_steps": self.refine_warp_steps,
                 "round_ms": list(self.round_ms), "fp64_segment_hist": list(self.fp64_segment_hist),
-                "fp64_segment_max": self.fp64_segment_max}
+                "fp64_segment_max": self.fp64_segment_max, "retired": self.retired}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.
@@ -94,7 +94,8 @@ EXPORTS = [
     "frg_config_default", "frg_create", "frg_destroy", "frg_last_error", "frg_set_config", "frg_track",
     "frg_track_async", "frg_coll_create", "frg_coll_destroy", "frg_coll_size", "frg_coll_get", "frg_coll_merge",
     "frg_coll_save", "frg_coll_load", "frg_codes_append", "frg_lambertw0", "frg_estimate_collected",
-    "frg_track_noalloc", "frg_track_rounds",
+    "frg_track_noalloc", "frg_track_rounds", "frg_set_mlp", "frg_track_features", "frg_mlp_param_count",
+    "frg_mlp_grad", "frg_mlp_train", "frg_mlp_predict",
 ]
 NOALLOC_MAX_TASKS = 1024
 
@@ -126,6 +127,18 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_track_rounds.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _I64, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(FrgStats)]
+    _F = ctypes.POINTER(ctypes.c_float)
+    lib.frg_set_mlp.argtypes = [ctypes.c_void_p, _F, _F, _F, ctypes.c_float, ctypes.c_int]
+    lib.frg_track_features.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _I64, ctypes.c_uint64,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _F,
+                                       ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(FrgStats)]
+    lib.frg_mlp_param_count.restype = ctypes.c_int
+    lib.frg_mlp_grad.argtypes = [_F, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, _F, _F, _F,
+                                 ctypes.POINTER(ctypes.c_double)]
+    lib.frg_mlp_train.argtypes = [_F, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, _F, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_float, ctypes.c_uint64, _F, ctypes.POINTER(ctypes.c_double)]
+    lib.frg_mlp_predict.argtypes = [_F, ctypes.c_int64, _F, _F]
     lib.frg_destroy.argtypes = [ctypes.c_void_p]
     lib.frg_last_error.argtypes = [ctypes.c_void_p]
     lib.frg_set_config.argtypes = [ctypes.c_void_p, ctypes.POINTER(FrgConfig)]
@@ -252,6 +265,38 @@ class Tracker:
                                        _ptr(codes), _ptr(resid), ctypes.byref(stats))
         self._check(st, "frg_track_rounds")
         return stats.as_dict()
+
+    def set_mlp(self, params=None, mu=None, inv_sigma=None, threshold: float = 0.99, every: int = 32):
+        """Switch early retirement on (params: frg_mlp_param_count() FP32 weights) or off (None)."""
+        if params is None:
+            self._check(self.lib.frg_set_mlp(self._ctx, None, None, None, ctypes.c_float(1.0), 1), "frg_set_mlp")
+            return
+        p = np.ascontiguousarray(params, np.float32)
+        m = np.ascontiguousarray(mu, np.float32)
+        s = np.ascontiguousarray(inv_sigma, np.float32)
+        _F = ctypes.POINTER(ctypes.c_float)
+        self._check(self.lib.frg_set_mlp(self._ctx, p.ctypes.data_as(_F), m.ctypes.data_as(_F), s.ctypes.data_as(_F),
+                                         ctypes.c_float(threshold), int(every)), "frg_set_mlp")
+
+    def track_features(self, fpm, paths_per_task, seed: int, max_checkpoints: int = 16, every: int = 32):
+        """frg_track that also returns every path's checkpoint features
+        (features [N, max_checkpoints, 32], nfeat [N])."""
+        fpm = np.ascontiguousarray(np.asarray(fpm, dtype=np.complex128).reshape(-1, NP))
+        ppt = np.ascontiguousarray(np.atleast_1d(np.asarray(paths_per_task, dtype=np.int64)))
+        n = int(ppt.sum())
+        roots = np.zeros((n, NV), np.complex128)
+        codes = np.zeros(n, np.int32)
+        resid = np.zeros(n, np.float64)
+        feats = np.zeros((n, max_checkpoints, 32), np.float32)
+        nfeat = np.zeros(n, np.int32)
+        stats = FrgStats()
+        st = self.lib.frg_track_features(self._ctx, fpm.ctypes.data, len(ppt), ppt.ctypes.data_as(_I64),
+                                         ctypes.c_uint64(seed), roots.ctypes.data, codes.ctypes.data,
+                                         resid.ctypes.data, feats.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                         nfeat.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(max_checkpoints),
+                                         int(every), ctypes.byref(stats))
+        self._check(st, "frg_track_features")
+        return TrackResult(roots, codes, None, resid, stats.as_dict()), feats, nfeat
 
     def track_async(self, fpm, paths_per_task, seed: int, roots, codes, yfinal=None, resid=None, stream=0):
         """Enqueue on a CUDA stream (device buffers only); returns immediately."""

@@ -11,6 +11,8 @@
 #include <vector>
 
 #include "../../include/frg_gb300.h"
+#include <cuda_bf16.h>
+
 #include "frg_kernels.h"
 #include "frg_rng.h"
 
@@ -81,6 +83,13 @@ struct frg_ctx {
   int last_rounds = 0;
   unsigned long long* h_counters = nullptr;  // pinned per-round counter copies (frg_track_rounds)
   size_t h_counters_n = 0;
+  // early-retirement network (frg_set_mlp) and checkpoint features (frg_track_features)
+  DevBuf mlp_w, mlp_norm, feat, nfeat;
+  float mlp_threshold = 1.f;
+  int mlp_every = 0;
+  bool mlp_on = false;
+  int feat_max = 0, feat_every = 0;
+  bool feat_on = false;
 };
 
 static frg_status fail(frg_ctx* ctx, frg_status s, const std::string& msg) {
@@ -210,7 +219,9 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
     sl->release();
     delete sl;
   }
-  for (DevBuf* b : {&ctx->fpm, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid}) b->release();
+  for (DevBuf* b : {&ctx->fpm, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->mlp_w, &ctx->mlp_norm,
+                    &ctx->feat, &ctx->nfeat})
+    b->release();
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -314,6 +325,21 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
   a.resid = d_resid;
   a.work = nullptr;
   a.counters = (unsigned long long*)sl.counters.p;
+  if (ctx->feat_on) {
+    a.feat = (float*)ctx->feat.p;
+    a.nfeat = (int32_t*)ctx->nfeat.p;
+    a.feat_max = ctx->feat_max;
+    a.feat_every = ctx->feat_every;
+    FRG_CUDA(ctx, cudaMemsetAsync(ctx->nfeat.p, 0, sizeof(int32_t) * (size_t)N, st));
+  }
+  if (ctx->mlp_on) {
+    a.mlp.w = (const __nv_bfloat16*)ctx->mlp_w.p;
+    a.mlp.mu = (const float*)ctx->mlp_norm.p;
+    a.mlp.inv_sigma = (const float*)ctx->mlp_norm.p + FRG_MLP_IN;
+    a.mlp.threshold = ctx->mlp_threshold;
+    a.mlp.every = ctx->mlp_every;
+    a.feat_every = ctx->mlp_every;
+  }
   const bool team = ctx->cfg.kernel_variant == FRG_KERNEL_TEAM;
   if (team) {  // start values for every path, generated once up front
     FRG_CUDA(ctx, sl.starts.ensure(sizeof(cx<double>) * frg::FRG_START_STRIDE * (size_t)N));
@@ -414,6 +440,7 @@ extern "C" frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntask
 // Adds one round's counters to stats (stats->paths and times are set by the caller).
 static void add_counters(frg_stats* st, const unsigned long long* cnt, bool mixed) {
   for (int k = 0; k < 8; ++k) st->codes[k] += (int64_t)cnt[k];
+  st->retired += (int64_t)cnt[36];
   st->ivp_solves += (int64_t)cnt[8];
   st->newton_iters += (int64_t)cnt[9];
   st->steps += (int64_t)cnt[10];
@@ -621,3 +648,57 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
   }
   return FRG_OK;
 }
+
+extern "C" frg_status frg_set_mlp(frg_ctx* ctx, const float* params, const float* mu, const float* inv_sigma,
+                                  float threshold, int every) {
+  if (!ctx) return FRG_ERR_ARG;
+  if (!params) {
+    ctx->mlp_on = false;
+    return FRG_OK;
+  }
+  if (!mu || !inv_sigma || every < 1 || !(threshold > 0.f && threshold <= 1.f))
+    return fail(ctx, FRG_ERR_ARG, "frg_set_mlp needs mu, inv_sigma, every >= 1 and 0 < threshold <= 1");
+  if (ctx->cfg.kernel_variant != FRG_KERNEL_TEAM)
+    return fail(ctx, FRG_ERR_ARG, "early retirement runs in the team kernels");
+  FRG_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<__nv_bfloat16> w(FRG_MLP_NPARAM);
+  for (int i = 0; i < FRG_MLP_NPARAM; ++i) w[i] = __float2bfloat16_rn(params[i]);
+  std::vector<float> norm(2 * FRG_MLP_IN);
+  for (int i = 0; i < FRG_MLP_IN; ++i) { norm[i] = mu[i]; norm[FRG_MLP_IN + i] = inv_sigma[i]; }
+  FRG_CUDA(ctx, ctx->mlp_w.ensure(sizeof(__nv_bfloat16) * FRG_MLP_NPARAM));
+  FRG_CUDA(ctx, ctx->mlp_norm.ensure(sizeof(float) * 2 * FRG_MLP_IN));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->mlp_w.p, w.data(), sizeof(__nv_bfloat16) * FRG_MLP_NPARAM, cudaMemcpyHostToDevice));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->mlp_norm.p, norm.data(), sizeof(float) * 2 * FRG_MLP_IN, cudaMemcpyHostToDevice));
+  ctx->mlp_threshold = threshold;
+  ctx->mlp_every = every;
+  ctx->mlp_on = true;
+  return FRG_OK;
+}
+
+extern "C" frg_status frg_track_features(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                                         uint64_t seed, double* roots, int32_t* codes, double* resid,
+                                         float* features, int32_t* nfeat, int max_checkpoints, int every,
+                                         frg_stats* stats) {
+  if (!ctx) return FRG_ERR_ARG;
+  if (!features || !nfeat || max_checkpoints < 1 || every < 1)
+    return fail(ctx, FRG_ERR_ARG, "frg_track_features needs features, nfeat, max_checkpoints >= 1, every >= 1");
+  if (ctx->cfg.kernel_variant != FRG_KERNEL_TEAM)
+    return fail(ctx, FRG_ERR_ARG, "checkpoint features come from the team kernels");
+  int64_t N = 0;
+  for (int k = 0; k < ntasks && paths_per_task; ++k) N += paths_per_task[k];
+  if (N <= 0) return frg_track(ctx, fpm, ntasks, paths_per_task, seed, roots, codes, nullptr, resid, stats);
+  FRG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t fb = sizeof(float) * FRG_MLP_IN * (size_t)max_checkpoints * (size_t)N;
+  FRG_CUDA(ctx, ctx->feat.ensure(fb));
+  FRG_CUDA(ctx, ctx->nfeat.ensure(sizeof(int32_t) * (size_t)N));
+  ctx->feat_on = true;
+  ctx->feat_max = max_checkpoints;
+  ctx->feat_every = every;
+  frg_status s = frg_track(ctx, fpm, ntasks, paths_per_task, seed, roots, codes, nullptr, resid, stats);
+  ctx->feat_on = false;
+  if (s != FRG_OK) return s;
+  FRG_CUDA(ctx, cudaMemcpy(nfeat, ctx->nfeat.p, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost));
+  FRG_CUDA(ctx, cudaMemcpy(features, ctx->feat.p, fb, cudaMemcpyDeviceToHost));
+  return FRG_OK;
+}
+

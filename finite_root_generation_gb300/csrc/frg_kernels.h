@@ -7,6 +7,7 @@
 #include "../../include/frg_gb300.h"
 #include "frg_complex.cuh"
 #include "frg_df.cuh"
+#include "frg_mlp.cuh"
 
 #ifndef FRG_TRACK_THREADS
 #define FRG_TRACK_THREADS 64
@@ -65,6 +66,11 @@ struct TrackArgs {
   int64_t* back_list;           // FP64 kernel: paths handed back to FP32 (null: none, e.g. the last round)
   unsigned long long* back_count;
   int lo_keep_ill;              // FP32 kernel: 1 = no hand-off for ill-conditioned steps (last round)
+  float* feat;                  // optional: FRG_MLP_IN features per checkpoint, feat_max checkpoints per path
+  int32_t* nfeat;               // checkpoints written per path (zeroed before launch)
+  int feat_max;
+  int feat_every;               // checkpoint every this many accepted steps (features and retirement)
+  MlpDevice mlp;                // early-retirement network (mlp.w null: off)
 };
 
 }  // namespace frg

@@ -183,6 +183,75 @@ __device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, i
   __syncwarp(tmask);
 }
 
+// Tracking features of a path at a checkpoint (an accepted step), the early-retirement
+// network's input: progress in t, step sizes now and at the last two checkpoints,
+// condition estimates, the homogenizer's share |Z0| / max|Z| (which goes to 0 on
+// paths diverging to infinity), step and rejection counts, patch switches and the
+// corrector's behaviour. One lane computes them from the shared state.
+template <typename P>
+__device__ void path_features(const cx<P>* Yc, double s, double rmax, int step, int ministep, uint64_t rng_index,
+                              double ck_t1, double ck_t2, double ck_s1, double ck_s2, bool fp64, int n_ivp,
+                              int n_newton, double residual, int streak, int tstepQ, int bounces, float* x) {
+  double zmax = 0.0;
+  for (int e = 0; e < 21; ++e) {
+    const cd v = cd(Yc[e]);
+    zmax = fmax(zmax, sqrt(cnorm2(v)));
+  }
+  const double z0 = sqrt(cnorm2(cd(Yc[21])));
+  const double t = double(Yc[22].re);
+  const auto lg = [](double v) { return (float)log10(fmax(v, 1e-30)); };
+  for (int k = 0; k < FRG_MLP_IN; ++k) x[k] = 0.f;
+  x[0] = (float)t;
+  x[1] = lg(fmax(1.0 - t, 1e-16));
+  x[2] = lg(s);
+  x[3] = lg(fmax(rmax, 1.0));
+  x[4] = lg(z0 / fmax(zmax, 1e-300));
+  x[5] = lg(zmax);
+  x[6] = step * 1e-3f;
+  x[7] = ministep * 1e-3f;
+  x[8] = (float)(ministep - 2 * step) / (float)(ministep > 0 ? ministep : 1);
+  x[9] = (float)((double)(rng_index > 92 ? rng_index - 92 : 0) / 46.0 * 0.1);
+  x[10] = (float)(t - ck_t1);
+  x[11] = lg(fmax(t - ck_t1, 1e-16));
+  x[12] = (float)(ck_t1 - ck_t2);
+  x[13] = lg(ck_s1 > 0 ? ck_s1 : s);
+  x[14] = lg(ck_s2 > 0 ? ck_s2 : s);
+  x[15] = fp64 ? 1.f : 0.f;
+  x[16] = (float)n_newton / (float)(n_ivp > 0 ? n_ivp : 1);
+  x[17] = lg(residual);
+  x[18] = streak * 0.1f;
+  x[19] = (float)tstepQ;
+  x[20] = bounces * 0.125f;
+}
+
+// One lane's work at a checkpoint: record the features and/or score them with the
+// network; returns 1 to retire the path. Not inlined, so its arrays stay off the
+// tracking loop's registers.
+template <typename P>
+__device__ __noinline__ int checkpoint(const TrackArgs& a, const cx<P>* Yc, int64_t id, double s, double rmax,
+                                       int step, int ministep, uint64_t rng_index, double ck_t1, double ck_t2,
+                                       double ck_s1, double ck_s2, bool fp64, int n_ivp, int n_newton,
+                                       double residual, int streak, int tstepQ, int bounces) {
+  float x[FRG_MLP_IN];
+  path_features<P>(Yc, s, rmax, step, ministep, rng_index, ck_t1, ck_t2, ck_s1, ck_s2, fp64, n_ivp, n_newton,
+                   residual, streak, tstepQ, bounces, x);
+  if (a.feat && a.nfeat) {
+    const int k = a.nfeat[id];
+    if (k < a.feat_max) {
+      float* dst = a.feat + ((size_t)id * a.feat_max + k) * FRG_MLP_IN;
+      for (int f = 0; f < FRG_MLP_IN; ++f) dst[f] = x[f];
+      a.nfeat[id] = k + 1;
+    }
+  }
+  if (!a.mlp.w) return 0;
+  for (int f = 0; f < FRG_MLP_IN; ++f) x[f] = (x[f] - a.mlp.mu[f]) * a.mlp.inv_sigma[f];
+  float z[FRG_MLP_OUT];
+  mlp_logits(a.mlp.w, x, z);
+  const int retire = mlp_prob(z, 1) >= a.mlp.threshold;
+  if (retire && a.counters) atomicAdd(&a.counters[36], 1ull);
+  return retire;
+}
+
 template <int MODE, typename T, typename P = typename PointOf<T>::type>
 __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -228,6 +297,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   bool hires = !LO;
   T res_prev = T(0);
   int good = 0, bounces = 0, seg = 0;
+  // checkpoint history (features of the early-retirement network)
+  double ck_t1 = 0.0, ck_t2 = 0.0;
+  float ck_s1 = 0.f, ck_s2 = 0.f, ck_rmax = 0.f;
+  const bool checkpoints = a.feat_every > 0 && (a.feat != nullptr || a.mlp.w != nullptr);
   unsigned long long fp64_solves = 0;
   // cycle accounting (lane 0 of each warp): fetch, setup, linear step, transitions;
   // warp steps and active-team steps
@@ -277,6 +350,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       }
       code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
       good = 0; bounces = 0; seg = 0;
+      ck_t1 = 0.0; ck_t2 = 0.0; ck_s1 = 0.f; ck_s2 = 0.f; ck_rmax = 0.f;
       if (MODE == MODE_RESUME || lo_resume) {
         const Handoff& h = a.handoff[id];
         for (int e = g; e < NY; e += TEAM) {
@@ -372,6 +446,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     }
     if (phase == PH_IDLE) continue;
     if (!LO) ++fp64_solves;
+    if (checkpoints) ck_rmax = fmaxf(ck_rmax, (float)r.ratio);
     if (MODE == MODE_RESUME) {
       good = (r.ratio < T(c.cond_switch * 1e-2)) ? good + 1 : 0;
       ++seg;
@@ -493,7 +568,19 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
             if (s > T(c.s_max)) s = T(c.s_max);
             else if (s < T(c.s_min)) s = T(c.s_min * 0.9);
             step++;
-            if (step == c.max_steps) { code = 1; finished = true; }
+            if (checkpoints && step % a.feat_every == 0) {
+              // checkpoint: record the features and/or let the network retire the path
+              int retire = 0;
+              __syncwarp(tmask);
+              if (g == 0)
+                retire = checkpoint<P>(a, S.Yc, id, double(s), ck_rmax, step, ministep, rng_index, ck_t1, ck_t2,
+                                       ck_s1, ck_s2, !LO, n_ivp, n_newton, double(residual), streak, tstepQ, bounces);
+              retire = __shfl_sync(tmask, retire, 0, TEAM);
+              ck_t2 = ck_t1; ck_t1 = double(S.Yc[22].re); ck_s2 = ck_s1; ck_s1 = float(s); ck_rmax = 0.f;
+              if (retire) { code = 2; finished = true; }  // retired early: reported as a step-limit failure
+            }
+            if (finished) {
+            } else if (step == c.max_steps) { code = 1; finished = true; }
             else if (LO && !c.lo_endgame && double(S.YN[22].re) >= c.t_switch) handoff = 1;
             else if (MODE == MODE_RESUME && a.back_list && (good >= kBackSteps || seg >= kSegment) &&
                      bounces < kMaxBounces && (c.lo_endgame || double(S.YN[22].re) < c.t_switch))

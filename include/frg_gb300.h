@@ -134,6 +134,7 @@ typedef struct frg_stats {
   int64_t fp64_segment_hist[6]; /* mixed: paths leaving an FP64 launch after <100, <300, <1000, <3000,
                                    <10000, >=10000 FP64 solves in it */
   int64_t fp64_segment_max;     /* mixed: most FP64 solves one path spent in one FP64 launch */
+  int64_t retired;              /* paths the early-retirement network ended (reported as code 2) */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;
@@ -180,6 +181,37 @@ frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const in
 frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
                             int nrounds, const uint64_t* seeds, int depth, double* roots, int32_t* codes,
                             double* resid, frg_stats* stats);
+
+/* Early retirement (no counterpart in the reference). A 32 -> 64 -> 64 -> 3 ReLU network
+ * (BF16 weights, FP32 sums) scores a path's tracking features every `every` accepted
+ * steps; a path whose probability of failing (no finite root with residual <= 1e-10)
+ * reaches `threshold` is ended and reported as code 2. params: FP32 weights in the
+ * layout of frg_mlp_param_count() (W1[64][32] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]);
+ * mu, inv_sigma: the 32 features' standardisation. params = NULL switches it off. */
+frg_status frg_set_mlp(frg_ctx* ctx, const float* params, const float* mu, const float* inv_sigma, float threshold,
+                       int every);
+
+/* frg_track (host or device outputs, no yfinal) that also records each path's
+ * checkpoint features: up to max_checkpoints vectors of 32 floats per path, one every
+ * `every` accepted steps, into features[N][max_checkpoints][32] (host), their count in
+ * nfeat[N]. The training data of the early-retirement network. */
+frg_status frg_track_features(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
+                              uint64_t seed, double* roots, int32_t* codes, double* resid, float* features,
+                              int32_t* nfeat, int max_checkpoints, int every, frg_stats* stats);
+
+/* The network's training and batch inference, with the library's own CUDA kernels on
+ * the current device. X: n x 32 standardised features (host), y: classes 0 new root,
+ * 1 fails, 2 duplicate root. frg_mlp_grad: mean class-weighted cross entropy and its
+ * gradient with respect to the BF16-rounded weights (host outputs). frg_mlp_train:
+ * Adam on shuffled mini-batches from `params` (all zero: He-normal start drawn from
+ * `seed`); params is updated in place, epoch_loss (optional) gets each epoch's mean
+ * loss. frg_mlp_predict: n x 3 class probabilities. */
+int frg_mlp_param_count(void);
+frg_status frg_mlp_grad(const float* X, const int32_t* y, int64_t n, const float* params, const float* class_w,
+                        float* grad, double* loss);
+frg_status frg_mlp_train(const float* X, const int32_t* y, int64_t n, const float* class_w, int epochs, int batch,
+                         float lr, uint64_t seed, float* params, double* epoch_loss);
+frg_status frg_mlp_predict(const float* X, int64_t n, const float* params, float* probs);
 
 /* Plain FP64 tracking that allocates no device memory. No counterpart in the
  * reference: it is for callers that may not call cudaMalloc / cudaFree, such as code
