@@ -82,7 +82,7 @@ __device__ __forceinline__ T team_min(unsigned mask, T v) {
 // YN (corrector iterate) are in the point type (FP64, or double-float in the FP32
 // stage, whose corrector refines on double-float residuals with an FP32 solve);
 // directions, patches and stage vectors are in the working precision T. U/Urhs hold the reduced system's
-// upper factor for the back substitution. The 32-byte pad makes the stride between
+// upper factor for the back substitution. The 32-byte tail makes the stride between
 // teams 32 bytes past a multiple of 128, so the four teams of a warp reading "the
 // same" field hit different bank groups.
 template <typename T, typename P = typename PointOf<T>::type>
@@ -93,7 +93,12 @@ struct Smem {
   cx<T> k[8][VS];
   cx<T> U[16][16];
   cx<T> Urhs[16];
-  unsigned char pad[32];
+  // Checkpoint history of the early-retirement features (lane 0 only). These 32 bytes
+  // also make the stride between teams 32 bytes past a multiple of 128.
+  double ck_t[2];   // t at the last two checkpoints
+  float ck_s[2];    // step sizes at the last two checkpoints
+  float ck_rmax;    // largest condition estimate since the last checkpoint
+  float ck_unused;
 };
 
 // Parameter values a lane needs for its group: index 0 P0, 1 Pc0, 2 Pj, 3 Pcj, 4 Qj, 5 Qcj.

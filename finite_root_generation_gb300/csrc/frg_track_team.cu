@@ -222,6 +222,8 @@ __device__ void path_features(const cx<P>* Yc, double s, double rmax, int step, 
   x[18] = streak * 0.1f;
   x[19] = (float)tstepQ;
   x[20] = bounces * 0.125f;
+  for (int k = 0; k < FRG_MLP_IN; ++k)  // non-finite inputs (an infinite condition estimate, a NaN residual)
+    x[k] = (x[k] - x[k] == 0.f) ? fminf(fmaxf(x[k], -100.f), 100.f) : 100.f;
 }
 
 // One lane's work at a checkpoint: record the features and/or score them with the
@@ -297,9 +299,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   bool hires = !LO;
   T res_prev = T(0);
   int good = 0, bounces = 0, seg = 0;
-  // checkpoint history (features of the early-retirement network)
-  double ck_t1 = 0.0, ck_t2 = 0.0;
-  float ck_s1 = 0.f, ck_s2 = 0.f, ck_rmax = 0.f;
+  // checkpoints of the early-retirement network (history kept in S.ck_*)
   const bool checkpoints = a.feat_every > 0 && (a.feat != nullptr || a.mlp.w != nullptr);
   unsigned long long fp64_solves = 0;
   // cycle accounting (lane 0 of each warp): fetch, setup, linear step, transitions;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       }
       code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
       good = 0; bounces = 0; seg = 0;
-      ck_t1 = 0.0; ck_t2 = 0.0; ck_s1 = 0.f; ck_s2 = 0.f; ck_rmax = 0.f;
+      if (g == 0) { S.ck_t[0] = S.ck_t[1] = 0.0; S.ck_s[0] = S.ck_s[1] = 0.f; S.ck_rmax = 0.f; }
       if (MODE == MODE_RESUME || lo_resume) {
         const Handoff& h = a.handoff[id];
         for (int e = g; e < NY; e += TEAM) {
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     }
     if (phase == PH_IDLE) continue;
     if (!LO) ++fp64_solves;
-    if (checkpoints) ck_rmax = fmaxf(ck_rmax, (float)r.ratio);
+    if (checkpoints && g == 0) S.ck_rmax = fmaxf(S.ck_rmax, (float)r.ratio);
     if (MODE == MODE_RESUME) {
       good = (r.ratio < T(c.cond_switch * 1e-2)) ? good + 1 : 0;
       ++seg;
@@ -573,10 +573,14 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
               int retire = 0;
               __syncwarp(tmask);
               if (g == 0)
-                retire = checkpoint<P>(a, S.Yc, id, double(s), ck_rmax, step, ministep, rng_index, ck_t1, ck_t2,
-                                       ck_s1, ck_s2, !LO, n_ivp, n_newton, double(residual), streak, tstepQ, bounces);
+                retire = checkpoint<P>(a, S.Yc, id, double(s), S.ck_rmax, step, ministep, rng_index, S.ck_t[0],
+                                       S.ck_t[1], S.ck_s[0], S.ck_s[1], !LO, n_ivp, n_newton, double(residual),
+                                       streak, tstepQ, bounces);
               retire = __shfl_sync(tmask, retire, 0, TEAM);
-              ck_t2 = ck_t1; ck_t1 = double(S.Yc[22].re); ck_s2 = ck_s1; ck_s1 = float(s); ck_rmax = 0.f;
+              if (g == 0) {
+                S.ck_t[1] = S.ck_t[0]; S.ck_t[0] = double(S.Yc[22].re);
+                S.ck_s[1] = S.ck_s[0]; S.ck_s[0] = float(s); S.ck_rmax = 0.f;
+              }
               if (retire) { code = 2; finished = true; }  // retired early: reported as a step-limit failure
             }
             if (finished) {

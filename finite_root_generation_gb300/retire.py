@@ -42,17 +42,40 @@ def path_labels(roots, codes, resid, dup_tol=1e-6):
     return y
 
 
-def training_set(tracker, fpm, paths_per_task, seeds, max_checkpoints=16, every=32):
-    """Checkpoint features X [m, 32] and labels y [m] from rounds tracked by `tracker`
-    (the plain FP64 tracker for teaching), one round per seed."""
-    xs, ys = [], []
+def training_set(tracker, fpm, paths_per_task, seeds, max_checkpoints=64, every=32):
+    """Checkpoint features X [m, 32], labels y [m] and the path of every checkpoint
+    (groups [m], unique across rounds) from rounds tracked by `tracker` (the plain FP64
+    tracker for teaching), one round per seed."""
+    xs, ys, gs = [], [], []
+    base = 0
     for sd in seeds:
         res, feats, nfeat = tracker.track_features(fpm, paths_per_task, sd, max_checkpoints, every)
         lab = path_labels(res.roots, res.codes, res.resid)
         mask = np.arange(max_checkpoints)[None, :] < nfeat[:, None]
         xs.append(feats[mask])
         ys.append(np.repeat(lab, nfeat))
-    return np.concatenate(xs).astype(np.float32), np.concatenate(ys).astype(np.int32)
+        gs.append(np.repeat(np.arange(len(nfeat), dtype=np.int64) + base, nfeat))
+        base += len(nfeat)
+    return (np.concatenate(xs).astype(np.float32), np.concatenate(ys).astype(np.int32),
+            np.concatenate(gs))
+
+
+def calibrate(model, X, y, groups, max_good_frac=1e-3):
+    """Smallest threshold at which at most `max_good_frac` of the paths that do not fail
+    (classes 0 and 2) would be retired at some checkpoint, from held-out checkpoints;
+    1.0 (never retire) when no threshold below it qualifies."""
+    p1 = model.predict(X)[:, 1].astype(np.float64)
+    paths, inv = np.unique(groups, return_inverse=True)
+    pmax = np.zeros(len(paths))
+    np.maximum.at(pmax, inv, p1)
+    fails = np.zeros(len(paths), bool)
+    fails[inv[y == 1]] = True
+    good = np.sort(pmax[~fails])
+    if len(good) == 0:
+        return 1.0
+    k = int(np.floor(max_good_frac * len(good)))
+    thr = float(np.nextafter(good[len(good) - 1 - k], np.inf)) if k < len(good) else 0.0
+    return min(max(thr, 0.5), 1.0)
 
 
 @dataclass
@@ -81,7 +104,7 @@ class Retirement:
 
 
 def standardisation(X):
-    X = np.asarray(X, np.float64)
+    X = np.nan_to_num(np.asarray(X, np.float64), nan=100.0, posinf=100.0, neginf=-100.0)
     mu = X.mean(axis=0)
     sd = X.std(axis=0)
     inv = np.where(sd > 1e-12, 1.0 / np.maximum(sd, 1e-12), 0.0)

@@ -61,18 +61,22 @@ def test_training_learns_a_separable_rule():
 
 
 def test_retirement_gain_over_plain_tracker():
-    """Train on plain-FP64 tracks of one round, then track another round with and
-    without retirement: the network must cut work and keep the distinct roots."""
+    """Train on plain-FP64 tracks of three rounds, calibrate the threshold on a fourth
+    (at most 0.1 % of the paths that do not fail would be retired), then track a fifth
+    round with and without retirement: the network must cut work and keep the roots."""
     frg_build.build()
     task = precision_point_task(1, "disk")
     base = dict(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=1e-8)
-    n = 8192
+    n, every = 16384, 32
     with frg.Tracker(frg.default_config(**base)) as t:
-        X, y = retire.training_set(t, task, [n], seeds=[101, 102], max_checkpoints=24, every=8)
-    assert (y == 1).sum() > 20 and (y == 0).sum() > 1000
-    model, losses = retire.train(X, y, epochs=10, batch=2048, lr=2e-3, seed=3, threshold=0.98, every=8,
+        X, y, _ = retire.training_set(t, task, [n], seeds=[101, 102, 103], max_checkpoints=64, every=every)
+        Xc, yc, gc = retire.training_set(t, task, [n], seeds=[104], max_checkpoints=64, every=every)
+    assert np.all(np.isfinite(X)) and (y == 1).sum() > 50 and (y == 0).sum() > 10000
+    model, losses = retire.train(X, y, epochs=12, batch=2048, lr=2e-3, seed=3, every=every,
                                  class_w=np.array([1.0, 2.0, 1.0], np.float32))
     assert losses[-1] < losses[0]
+    model.threshold = retire.calibrate(model, Xc, yc, gc, max_good_frac=1e-3)
+    assert model.threshold < 1.0
     with frg.Tracker(frg.default_config(**base)) as t:
         plain = t.track(task, [n], 777, want_resid=True)
         model.apply(t)
@@ -81,6 +85,9 @@ def test_retirement_gain_over_plain_tracker():
     b = distinct_roots(ret.roots, ret.codes, ret.resid)
     work_plain = plain.stats["ivp_solves"] + plain.stats["newton_iters"]
     work_ret = ret.stats["ivp_solves"] + ret.stats["newton_iters"]
+    print(f"retired {ret.stats['retired']} paths at threshold {model.threshold:.4f}; solves {work_ret} vs "
+          f"{work_plain}; time {ret.stats['track_ms']:.0f} vs {plain.stats['track_ms']:.0f} ms; "
+          f"recall {recall(a, b):.5f}")
     assert ret.stats["retired"] > 0
     assert work_ret < work_plain
     assert recall(a, b) >= 0.995
