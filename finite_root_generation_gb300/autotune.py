@@ -3,7 +3,7 @@
 For one workload (a task and a round size) it times every candidate setting on a
 sample of rounds, keeps those whose distinct finite roots recall at least
 `target_recall` of the plain FP64 tracker's on the same seeds (the plain tracker is
-the judge), picks the highest distinct-roots-per-second, re-checks that choice on
+the reference point), picks the highest distinct-roots-per-second, re-checks that choice on
 fresh seeds, and caches it per GPU model and workload in a JSON file.
 
 Searched dimensions (each a field of frg_config, or the rounds in flight of
@@ -12,6 +12,7 @@ frg_track_rounds):
   blocks_per_sm   resident blocks per SM (0 = the occupancy maximum)
   precision       FP64, or mixed with the FP32 stage's point type lo_points 0/1
   cond_switch     the condition estimate above which a step goes to FP64
+  fp64_budget     FP64 solves a path may spend before it is ended
   depth           rounds in flight
 """
 from __future__ import annotations
@@ -33,7 +34,8 @@ DEFAULT_SPACE = {
     "precision": [PREC_MIXED],
     "lo_points": [0, 1],
     "cond_switch": [1e5, 1e6],
-    "depth": [2, 3],
+    "fp64_budget": [0, 10000],
+    "depth": [2, 4],
 }
 
 
@@ -93,7 +95,8 @@ def autotune(task, n=8192, rounds=2, base=None, space=None, target_recall=0.995,
     results = []
     for values in itertools.product(*(space[k] for k in names)):
         cand = dict(zip(names, values))
-        if cand.get("precision") == PREC_FP64 and (cand.get("lo_points", 0) or cand.get("cond_switch", 1e5) != 1e5):
+        if cand.get("precision") == PREC_FP64 and (cand.get("lo_points", 0) or cand.get("cond_switch", 1e5) != 1e5
+                                                  or cand.get("fp64_budget", 0)):
             continue  # FP64 ignores the mixed-precision fields
         if cand.get("kernel_variant") == KERNEL_THREAD and cand.get("lo_points", 0):
             continue  # the point type option exists for the team kernels only
