@@ -72,7 +72,7 @@ struct frg_ctx {
   int device = 0;
   frg_config cfg;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evmid = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int sm_count = 0;
   int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM of each thread-per-path kernel mode
   int team_blocks_per_sm[4] = {0, 0, 0, 0};
@@ -188,7 +188,6 @@ extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int devic
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-  if (e == cudaSuccess) e = cudaEventCreate(&ctx->evmid);
   for (int m = 0; m < 3 && e == cudaSuccess; ++m) {
     e = frg_track_occupancy(m, &ctx->blocks_per_sm[m]);
     if (ctx->blocks_per_sm[m] < 1) ctx->blocks_per_sm[m] = 1;
@@ -226,7 +225,6 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->round_ev) cudaEventDestroy(e);
-  if (ctx->evmid) cudaEventDestroy(ctx->evmid);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -15,9 +15,6 @@
 #ifndef FRG_TEAM_THREADS
 #define FRG_TEAM_THREADS 64
 #endif
-#ifndef FRG_MIXED_ROUNDS
-#define FRG_MIXED_ROUNDS 8  // FP32/FP64 rounds of a mixed-precision call
-#endif
 
 namespace frg {
 
