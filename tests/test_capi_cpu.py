@@ -125,3 +125,35 @@ def test_tracker_without_gpu_raises(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(frg.FrgError):
         frg.Tracker()
+
+
+def test_invalid_configs_rejected_before_any_cuda_call():
+    """frg_create checks the configuration first, so bad settings fail with FRG_ERR_ARG
+    (-1) even on a machine without a GPU."""
+    import ctypes
+
+    lib = frg.load()
+    bad = [dict(lo_refine=3), dict(lo_points=2), dict(fp64_budget=-1), dict(mixed_rounds=65), dict(path_offset=-1),
+           dict(lo_final=2), dict(fp64_segment=-5), dict(handback_good=-1), dict(precision=7),
+           dict(kernel_variant=9), dict(rk_tol=0.0), dict(newt_attempts=0),
+           dict(precision=frg.PREC_MIXED, cond_switch=0.5)]
+    for kw in bad:
+        cfg = frg.default_config(**kw)
+        ctx = ctypes.c_void_p()
+        assert lib.frg_create(ctypes.byref(ctx), ctypes.byref(cfg), 0) == -1, kw
+        assert not ctx.value
+
+
+def test_noalloc_rejects_bad_arguments_without_a_gpu():
+    import ctypes
+
+    lib = frg.load()
+    lib.frg_track_noalloc.restype = ctypes.c_int
+    cfg = frg.default_config()
+    ppt = (ctypes.c_int64 * 1)(4)
+    assert lib.frg_track_noalloc(ctypes.byref(cfg), None, 1, ppt, ctypes.c_uint64(1), None, None, None, None) == -1
+    many = frg.NOALLOC_MAX_TASKS + 1
+    ppt_many = (ctypes.c_int64 * many)(*([1] * many))
+    buf = (ctypes.c_double * 8)()
+    assert lib.frg_track_noalloc(ctypes.byref(cfg), buf, many, ppt_many, ctypes.c_uint64(1), buf, buf, None,
+                                 None) == -1
