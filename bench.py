@@ -230,7 +230,20 @@ def _round_sets(roots, codes, resid, n, k):
             for i in range(k)]
 
 
-def _timed_rounds(torch, tracker, d_fpm, n, seeds, outs, depth, world):
+def workload_tasks(precision_point_task, ntasks, n):
+    """The tasks of a round and their path counts: one generic task (seed 1, points in
+    the unit disk) or, for ntasks > 1, tasks from seeds 0..ntasks-1 alternating points in
+    the unit disk and points along a random smooth closed curve (the batched uneven
+    workload), n paths split evenly."""
+    if ntasks <= 1:
+        return precision_point_task(TASK_SEED, "disk"), [n]
+    if n % ntasks:
+        raise SystemExit("--paths must be a multiple of --tasks")
+    tasks = np.stack([precision_point_task(i, "disk" if i % 2 == 0 else "curve") for i in range(ntasks)])
+    return tasks, [n // ntasks] * ntasks
+
+
+def _timed_rounds(torch, tracker, d_fpm, ppt, seeds, outs, depth, world):
     """K rounds through frg_track_rounds (device buffers, `depth` rounds in flight),
     bracketed by a barrier and a synchronize on both sides. The library times the
     span with CUDA events on its launching streams (first launch to the last round's
@@ -242,7 +255,7 @@ def _timed_rounds(torch, tracker, d_fpm, n, seeds, outs, depth, world):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
-    st = tracker.track_rounds(d_fpm, [n], seeds, roots, codes, resid=resid, depth=depth)
+    st = tracker.track_rounds(d_fpm, ppt, seeds, roots, codes, resid=resid, depth=depth)
     ev1.record()
     torch.cuda.synchronize()
     if world > 1:
@@ -261,7 +274,7 @@ def run_ours(args, rank, world):
     frg_build.build()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    task = precision_point_task(TASK_SEED, "disk")
+    task, ppt = workload_tasks(precision_point_task, args.tasks, args.paths)
     n, k, depth = args.paths, args.steps, args.depth
     chosen_cfg = workload_config(frg, frg.PREC_MIXED)
     for key, v in _chosen_overrides().items():
@@ -280,20 +293,21 @@ def run_ours(args, rank, world):
     seeds = [seed_of(i) for i in range(k)]
     # warm-up: W rounds of the chosen configuration and one of the plain one
     warm = [seed_of(-1 - i) for i in range(args.warmup)]
-    chosen.track_rounds(d_fpm, [n], warm, outs[0][: len(warm) * n], outs[1][: len(warm) * n],
+    chosen.track_rounds(d_fpm, ppt, warm, outs[0][: len(warm) * n], outs[1][: len(warm) * n],
                         resid=outs[2][: len(warm) * n], depth=depth)
-    plain.track_rounds(d_fpm, [min(n, 8192)], warm[:1], outs[0], outs[1], resid=outs[2], depth=1)
+    plain.track_rounds(d_fpm, [min(c, max(1, 8192 // len(ppt))) for c in ppt], warm[:1], outs[0], outs[1],
+                       resid=outs[2], depth=1)
     torch.cuda.synchronize()
 
     # ---- chosen configuration, inputs resident in HBM (value) ----
     c_outs = tuple(o[: k * n] for o in outs)
     with ClockSampler(dev) as clk:
-        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_fpm, n, seeds, c_outs, depth, world)
+        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_fpm, ppt, seeds, c_outs, depth, world)
     clocks = clk.summary()
     c_sets = _round_sets(*c_outs, n, k)
     # ---- plain FP64 on the same seeds, pipelined the same way (ratio and recall) ----
     kp = max(1, min(args.plain_steps, k))
-    p_st, _ = _timed_rounds(torch, plain, d_fpm, n, seeds[:kp], tuple(o[: kp * n] for o in outs), depth, world)
+    p_st, _ = _timed_rounds(torch, plain, d_fpm, ppt, seeds[:kp], tuple(o[: kp * n] for o in outs), depth, world)
     p_sets = _round_sets(*(o[: kp * n] for o in outs), n, kp)
     rec = [recall(p_sets[i], c_sets[i]) for i in range(kp)]
 
@@ -308,7 +322,7 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    chosen.track_rounds(task, [n], seeds, hr, hc, resid=he, depth=depth)
+    chosen.track_rounds(task, ppt, seeds, hr, hc, resid=he, depth=depth)
     R = hr.view(np.complex128)
     e2e_distinct = sum(len(distinct_roots(R[i * n:(i + 1) * n], hc[i * n:(i + 1) * n], he[i * n:(i + 1) * n],
                                           RESID_MAX)) for i in range(k))
@@ -357,15 +371,18 @@ def run_ours(args, rank, world):
     p_solves = (p_st["ivp_solves"] + p_st["newton_iters"]) / kp
     p_ms_round = p_st["stage_ms"][1] / kp
     plain_roof = p_solves * fps / (p_ms_round * 1e-3) / 1e12
-    h2d = 16 * 30 + 16 + 16
+    h2d = len(ppt) * (16 * 30 + 16 + 8) + 8  # task parameters, gammas, path offsets
     d2h = n * (16 * 21 + 4 + 8)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": k,
         "warmup": args.warmup, "ms_per_step": round(track_ms / k, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded task and start mechanisms)",
-        "config": {"workload": f"Stephenson II FRG rounds of {n} paths on 1 generic complex precision-point task "
-                               f"(seed {TASK_SEED}), complex-normal start mechanisms, random unit gamma per round; "
+        "config": {"workload": (f"Stephenson II FRG rounds of {n} paths on 1 generic complex precision-point task "
+                                f"(seed {TASK_SEED})" if len(ppt) == 1 else
+                                f"Stephenson II FRG rounds of {n} paths over {len(ppt)} tasks (seeds 0..{len(ppt) - 1}, "
+                                "points in the unit disk / along a random closed curve, alternating)")
+                               + ", complex-normal start mechanisms, random unit gamma per round; "
                                "FP64 sharpening check, canonical cognates, finite + residual <= 1e-10 checks, "
                                "duplicate removal",
                    "paths_per_step": n, "rounds_in_flight": depth,
@@ -470,6 +487,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8192)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--depth", type=int, default=4, help="rounds in flight")
+    ap.add_argument("--tasks", type=int, default=1, help="tasks per round (>1: the batched uneven workload)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
