@@ -593,35 +593,45 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
   for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, ev_start, 0));
   const size_t rb = sizeof(cx<double>) * 21 * (size_t)N, cb = sizeof(int32_t) * (size_t)N,
                eb = sizeof(double) * (size_t)N;
-  for (int r = 0; r < nrounds; ++r) {
-    Slot& sl = *ctx->slots[r % depth];
-    cudaStream_t st = sl.stream;
-    cx<double>* d_roots;
-    int32_t* d_codes;
-    double* d_resid = nullptr;
-    if (dev_out) {
-      d_roots = (cx<double>*)((char*)roots + rb * r);
-      d_codes = (int32_t*)((char*)codes + cb * r);
-      if (resid) d_resid = (double*)((char*)resid + eb * r);
-    } else {
-      FRG_CUDA(ctx, sl.roots.ensure(rb));
-      FRG_CUDA(ctx, sl.codes.ensure(cb));
-      d_roots = (cx<double>*)sl.roots.p;
-      d_codes = (int32_t*)sl.codes.p;
-      if (resid) { FRG_CUDA(ctx, sl.resid.ensure(eb)); d_resid = (double*)sl.resid.p; }
+  // on a failure part-way, rounds already enqueued must finish before the caller's
+  // buffers can be reused: drain every slot's stream, then report the first error
+  auto enqueue_all = [&]() -> frg_status {
+    for (int r = 0; r < nrounds; ++r) {
+      Slot& sl = *ctx->slots[r % depth];
+      cudaStream_t st = sl.stream;
+      cx<double>* d_roots;
+      int32_t* d_codes;
+      double* d_resid = nullptr;
+      if (dev_out) {
+        d_roots = (cx<double>*)((char*)roots + rb * r);
+        d_codes = (int32_t*)((char*)codes + cb * r);
+        if (resid) d_resid = (double*)((char*)resid + eb * r);
+      } else {
+        FRG_CUDA(ctx, sl.roots.ensure(rb));
+        FRG_CUDA(ctx, sl.codes.ensure(cb));
+        d_roots = (cx<double>*)sl.roots.p;
+        d_codes = (int32_t*)sl.codes.p;
+        if (resid) { FRG_CUDA(ctx, sl.resid.ensure(eb)); d_resid = (double*)sl.resid.p; }
+      }
+      cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
+      s = enqueue_track(ctx, sl, d_fpm, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
+                        rev);
+      if (s != FRG_OK) return s;
+      FRG_CUDA(ctx, cudaEventRecord(rev[per], st));
+      if (!dev_out) {  // host outputs: asynchronous when the caller's buffers are pinned
+        FRG_CUDA(ctx, cudaMemcpyAsync((char*)roots + rb * r, d_roots, rb, cudaMemcpyDeviceToHost, st));
+        FRG_CUDA(ctx, cudaMemcpyAsync((char*)codes + cb * r, d_codes, cb, cudaMemcpyDeviceToHost, st));
+        if (resid) FRG_CUDA(ctx, cudaMemcpyAsync((char*)resid + eb * r, d_resid, eb, cudaMemcpyDeviceToHost, st));
+      }
+      FRG_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters + (size_t)r * FRG_NCOUNTERS, sl.counters.p,
+                                    sizeof(unsigned long long) * FRG_NCOUNTERS, cudaMemcpyDeviceToHost, st));
     }
-    cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
-    s = enqueue_track(ctx, sl, d_fpm, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
-                      rev);
-    if (s != FRG_OK) return s;
-    FRG_CUDA(ctx, cudaEventRecord(rev[per], st));
-    if (!dev_out) {  // host outputs: asynchronous when the caller's buffers are pinned
-      FRG_CUDA(ctx, cudaMemcpyAsync((char*)roots + rb * r, d_roots, rb, cudaMemcpyDeviceToHost, st));
-      FRG_CUDA(ctx, cudaMemcpyAsync((char*)codes + cb * r, d_codes, cb, cudaMemcpyDeviceToHost, st));
-      if (resid) FRG_CUDA(ctx, cudaMemcpyAsync((char*)resid + eb * r, d_resid, eb, cudaMemcpyDeviceToHost, st));
-    }
-    FRG_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters + (size_t)r * FRG_NCOUNTERS, sl.counters.p,
-                                  sizeof(unsigned long long) * FRG_NCOUNTERS, cudaMemcpyDeviceToHost, st));
+    return FRG_OK;
+  };
+  s = enqueue_all();
+  if (s != FRG_OK) {
+    for (int d = 0; d < depth; ++d) cudaStreamSynchronize(ctx->slots[d]->stream);
+    return s;
   }
   for (int d = 0; d < depth; ++d) FRG_CUDA(ctx, cudaStreamSynchronize(ctx->slots[d]->stream));
   if (stats) {
