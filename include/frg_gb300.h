@@ -20,7 +20,8 @@
  *   - per-path codes: 0 success, 1 max steps, 2 max ministeps, 3 predictor step
  *     below s_min, 4 corrector failed at s_min, 5 sharpening failed
  *     (htpytrack.cu:85,95,100,159,216), 6 duplicate (frgsupport.cu:8), plus
- *     7 = tracked to an infinite root (only when frg_config.inf_tol > 0);
+ *     7 = tracked to an infinite root (only when frg_config.inf_tol > 0); code 2 also
+ *     marks paths ended by fp64_budget or by the early-retirement network;
  *   - buffers are owned by the caller and may be host or device memory.
  *
  * Errors: functions return frg_status; FRG_OK == 0, negative values are argument,
@@ -81,8 +82,9 @@ typedef struct frg_config {
   double gamma_re, gamma_im;
   double dup_tol;       /* absolute per-component duplicate tolerance */
   int precision;        /* FRG_PREC_FP64 (reference arithmetic) or FRG_PREC_MIXED */
-  double t_switch;      /* mixed: FP64 tracking once t exceeds this */
-  double cond_switch;   /* mixed: FP64 corrector when the LU pivot ratio exceeds this */
+  double t_switch;      /* mixed, lo_endgame = 0: FP64 tracking once t exceeds this */
+  double cond_switch;   /* mixed: a step whose condition estimate (the elimination's pivot ratios)
+                           exceeds this continues its path in FP64 */
   double inf_tol;       /* > 0: |Z0| / |Z| below this at t = 1 marks code 7 */
   int threads_per_block; /* 0 = tuned default */
   int blocks_per_sm;     /* 0 = tuned default */
@@ -90,9 +92,10 @@ typedef struct frg_config {
   int kernel_variant;    /* FRG_KERNEL_TEAM (8 lanes per path, default) or FRG_KERNEL_THREAD */
   int mixed_rounds;      /* mixed, team kernels: FP32/FP64 rounds; a path well conditioned again in
                             FP64 returns to FP32 in the next round (1 = no return) */
-  int lo_refine;         /* mixed: 1 = the FP32 corrector refines on double-float residuals to
-                            newt_tol; 2 = the same, but a refined iteration whose successor is
-                            predicted below newt_tol / 10 ends it; 0 = it stops at newt_tol_lo */
+  int lo_refine;         /* mixed: 1 = the FP32 corrector refines on residuals in the point type
+                            (lo_points) to newt_tol; 2 = the same, but a refined iteration whose
+                            successor is predicted below newt_tol / 10 ends it; 0 = it stops at
+                            newt_tol_lo */
   int lo_endgame;        /* mixed: 1 = the FP32 stage (with refinement) also runs the endgame and
                             sharpening, FP64 only for ill-conditioned steps; 0 = FP64 from t_switch */
   int64_t path_offset;   /* random stream of local path i is path_offset + i: shards of one round
@@ -130,7 +133,8 @@ typedef struct frg_stats {
   int64_t handbacks;       /* mixed: returns from FP64 to FP32 once well conditioned again */
   int64_t refine_solves;   /* mixed: FP32-stage corrector iterations on double-float residuals */
   int64_t refine_warp_steps; /* mixed: FP32-stage warp steps in which at least one path refined */
-  double round_ms[32];     /* mixed: FP32-stage and FP64-stage times of rounds 0..15, interleaved */
+  double round_ms[32];     /* mixed: FP32-stage and FP64-stage times, interleaved, of mixed rounds
+                              0..15 (frg_track) or of rounds 0..15 of the call (frg_track_rounds) */
   int64_t fp64_segment_hist[6]; /* mixed: paths leaving an FP64 launch after <100, <300, <1000, <3000,
                                    <10000, >=10000 FP64 solves in it */
   int64_t fp64_segment_max;     /* mixed: most FP64 solves one path spent in one FP64 launch */
