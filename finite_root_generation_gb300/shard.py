@@ -36,13 +36,19 @@ def shard_paths_per_task(paths_per_task, first: int, count: int) -> np.ndarray:
 
 
 def track_shard(tracker, fpm, paths_per_task, seed: int, rank: int, world: int, want_resid: bool = True):
-    """Track rank's share of a round with ``tracker`` (a Tracker); returns (first, TrackResult)."""
+    """Track rank's share of a round with ``tracker`` (a Tracker); returns (first, TrackResult).
+    The tracker's path_offset is restored afterwards."""
     first, count = shard_range(int(np.sum(paths_per_task)), rank, world)
     cfg = tracker.config
+    old = cfg.path_offset
     cfg.path_offset = first
     tracker.set_config(cfg)
-    return first, tracker.track(fpm, shard_paths_per_task(paths_per_task, first, count), seed,
-                                want_resid=want_resid)
+    try:
+        return first, tracker.track(fpm, shard_paths_per_task(paths_per_task, first, count), seed,
+                                    want_resid=want_resid)
+    finally:
+        cfg.path_offset = old
+        tracker.set_config(cfg)
 
 
 def gather_merge(collection, roots, codes, group=None):
