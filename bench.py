@@ -1,27 +1,32 @@
-"""Benchmark: distinct finite roots per second on one GB300.
+"""Benchmark: distinct finite roots per second on one GB300, chosen configuration vs
+plain FP64 (the metric of the mixed-precision tracker).
 
-Workload (one "step" = one round of the tracker): 65,536 paths on one generic
-precision-point task (seed 1: P_k and Pc_k uniform in the unit disk, crank rotations
-on the unit circle), start mechanisms from complex normal link/pivot values, a random
-unit-modulus gamma, sharpening to 1e-12 at t = 1 in FP64, canonical cognates, finite-root check
-(|Z0|/|Z| >= 1e-8), per-root residual, and duplicate removal in a root collection.
-A root counts when its path succeeded, it is finite, its row-scaled residual is
-<= 1e-10, and it is not a duplicate. Synthetic inputs: the reference ships no
+Workload (default, --workload c5): 1,048,576 paths over 128 tasks, 8,192 paths each.
+Task k (seeds 0..127) has its precision points in the unit disk (even k) or along a
+random smooth closed curve with 1% jitter (odd k); crank rotations on the unit circle.
+Start mechanisms from complex-normal link/pivot values, a random unit-modulus gamma per
+task and round, sharpening to 1e-12 at t = 1, canonical cognates, finite-root check
+(|Z0|/|Z| >= 1e-8) and per-root residual. A root counts when its path succeeded, it is
+finite, its row-scaled residual is <= 1e-10, and it is not a duplicate of a root already
+collected for its task in the timed region (one collection per task across all steps,
+the reference's cross-round merge, frg.cu:440). Synthetic inputs: the reference ships no
 benchmark data; tasks and starts are seeded.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--paths P] [--impl ours|reference]
+One step = one round of 8 tasks x 8,192 paths (65,536 paths): step s tracks tasks
+8 (s mod 16) .. 8 (s mod 16) + 7 with seed 1000003 + s, so 16 steps cover the whole
+1,048,576-path workload and later steps run further rounds on the same tasks.
 
-value    distinct finite roots / second over K rounds (steps) of the chosen configuration run
-         through frg_track_rounds with `--depth` rounds in flight (inputs resident in HBM, CUDA
-         events on the launching streams); the chosen configuration is mixed precision (FP32
-         team kernel with double-float refinement, FP64 for ill-conditioned steps and for
-         finishing every root). Plain FP64 on the same seeds, pipelined the same way, gives
-         `plain_fp64`, the speed-up and the recall
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c5|c4|c2] [--impl ours|reference]
+
+value    distinct finite roots / second over K steps of the chosen configuration run through
+         frg_track_rounds with --depth rounds in flight (task sets resident in HBM, CUDA events
+         on the launching streams). Plain FP64 over the same K steps, seeds and pipelining gives
+         plain_fp64, the speed-up and the recall of plain FP64's distinct roots.
 e2e      the same through the public C ABI with pinned host buffers: the task upload, tracking,
-         the copy of roots/codes/residuals back and the host duplicate merge of every round
---impl reference  times the reference algorithm's CPU implementation (the C
-         restatement in oracle/, the reference's own sources cannot be built on the GPU
-         host) on all host cores, on a bounded sample of the same workload.
+         the copy of roots/codes/residuals back and the host duplicate merge of every step
+--impl reference  the reference's own tracker sources built for the host (oracle/_ref,
+         staged reference sources; the oracle restatement where they are missing) on all host
+         cores, each step a bounded sample of the same step's tasks, seeds and path streams.
 Multi-GPU: paths are independent; N ranks each run the workload on their own GPU with
 their own seeds (weak scaling) and the job value is the sum over ranks.
 """
@@ -45,20 +50,72 @@ METRIC = "distinct finite roots/sec at >=99.5% recall, residual <=1e-10: chosen 
 UNIT = "roots/s"
 RESID_MAX = 1e-10
 INF_TOL = 1e-8
-TASK_SEED = 1
+DUP_TOL = 1e-6
+SEED_BASE = 1000003
+WARM_SEED_BASE = 7000001
+
+
+def _load_tasks_module():
+    """The task generator (numpy only), loaded by file path so that the reference arm
+    never imports the product package."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "frg_bench_tasks", os.path.join(ROOT, "finite_root_generation_gb300", "tasks.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+class Workload:
+    """Tasks, their path counts and the tasks of each step.
+
+    c5: 128 tasks (seeds 0..127, disk / curve alternating) x 8,192 paths, 8 tasks per step
+    c4: 64 tasks (seeds 0..63, disk / curve alternating) x 8,192 paths, 8 tasks per step
+    c2: 1 task (seed 1, disk) x 65,536 paths per step (rounds on one task, the reference's loop)"""
+
+    def __init__(self, name):
+        tm = _load_tasks_module()
+        self.name = name
+        if name == "c5":
+            ntasks, self.paths_per_task, self.tasks_per_step = 128, 8192, 8
+        elif name == "c4":
+            ntasks, self.paths_per_task, self.tasks_per_step = 64, 8192, 8
+        elif name == "c2":
+            ntasks, self.paths_per_task, self.tasks_per_step = 1, 65536, 1
+        else:
+            raise SystemExit(f"unknown workload {name}")
+        if name == "c2":
+            self.tasks = np.stack([tm.precision_point_task(1, "disk")])
+        else:
+            self.tasks = np.stack([tm.precision_point_task(k, "disk" if k % 2 == 0 else "curve")
+                                   for k in range(ntasks)])
+        self.ntasks = ntasks
+        self.blocks = ntasks // self.tasks_per_step
+        self.paths_per_step = self.paths_per_task * self.tasks_per_step
+
+    def step_tasks(self, s):
+        """Global task indices of step s."""
+        b = s % self.blocks
+        return list(range(b * self.tasks_per_step, (b + 1) * self.tasks_per_step))
+
+    def task_sets(self, steps):
+        """[len(steps), tasks_per_step, 30] task parameters of the given steps."""
+        return np.ascontiguousarray(np.stack([self.tasks[self.step_tasks(s)] for s in steps]))
+
+    def describe(self):
+        if self.name == "c2":
+            return ("Stephenson II FRG rounds of 65,536 paths on one generic complex precision-point task (seed 1, "
+                    "points in the unit disk)")
+        total = self.ntasks * self.paths_per_task
+        return (f"Stephenson II FRG, {total:,} paths over {self.ntasks} tasks ({self.paths_per_task:,} each; task "
+                f"seeds 0..{self.ntasks - 1}, precision points in the unit disk / along a random smooth closed curve "
+                f"with 1% jitter, alternating), one step = {self.tasks_per_step} tasks x {self.paths_per_task:,} "
+                f"paths, {self.blocks} steps per pass over all tasks")
 
 
 def workload_config(frg, precision):
     return frg.default_config(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=INF_TOL,
                               precision=precision)
-
-
-def count_distinct(frg, roots, codes, resid):
-    good = (codes == 0) & (resid <= RESID_MAX)
-    c = np.where(good, 0, np.where(codes == 0, 5, codes)).astype(np.int32)
-    coll = frg.Collection(1e-6)
-    out = coll.merge(roots, c)
-    return len(coll), out
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -212,42 +269,49 @@ def flops_per_solve():
 
 
 # ---------------------------------------------------------------------- our impl
-def _chosen_overrides():
-    """The chosen configuration on top of the workload's: mixed precision, the FP32
-    stage also running the endgame and sharpening (double-float refinement), FP64 for
+def _chosen_overrides(frg):
+    """The chosen configuration on top of the workload's (frg.CHOSEN): mixed precision, the
+    FP32 stage also running the endgame and sharpening (double-float refinement), FP64 for
     steps whose condition estimate exceeds 1e5 and for finishing every root, and at most
     10,000 FP64 solves per path (a path still going after that ends as a step-limit
     failure; such paths are crawling near a singularity and set the FP64 tail)."""
-    return dict(mixed_rounds=1, lo_endgame=1, cond_switch=1e5, lo_points=1, fp64_budget=10000)
+    return dict(frg.CHOSEN)
 
 
-def _round_sets(roots, codes, resid, n, k):
-    from finite_root_generation_gb300.metrics import distinct_roots
-    R = roots.cpu().numpy().view(np.complex128)
-    C = codes.cpu().numpy()
-    E = resid.cpu().numpy()
-    return [distinct_roots(R[i * n:(i + 1) * n], C[i * n:(i + 1) * n], E[i * n:(i + 1) * n], RESID_MAX)
-            for i in range(k)]
+class TaskCollections:
+    """One root collection per task across all steps (the reference merges every round
+    into one collection, frg.cu:440); counts distinct finite roots."""
+
+    def __init__(self, make_collection, ntasks):
+        self.make = make_collection
+        self.colls = {}
+        self.ntasks = ntasks
+
+    def merge_step(self, wl, s, roots, codes, resid):
+        """roots [P, 21] complex, codes [P], resid [P] of step s (paths_per_task per task)."""
+        ppt = wl.paths_per_task if roots.shape[0] == wl.paths_per_step else roots.shape[0] // wl.tasks_per_step
+        for i, k in enumerate(wl.step_tasks(s)):
+            sl = slice(i * ppt, (i + 1) * ppt)
+            good = (codes[sl] == 0) & (resid[sl] <= RESID_MAX)
+            c = np.where(good, 0, 5).astype(np.int32)
+            if k not in self.colls:
+                self.colls[k] = self.make()
+            self.colls[k].merge(roots[sl], c)
+
+    def distinct(self):
+        return sum(len(c) for c in self.colls.values())
+
+    def roots_of(self, k):
+        c = self.colls.get(k)
+        return c.roots() if c is not None else np.zeros((0, 21), np.complex128)
 
 
-def workload_tasks(precision_point_task, ntasks, n):
-    """The tasks of a round and their path counts: one generic task (seed 1, points in
-    the unit disk) or, for ntasks > 1, tasks from seeds 0..ntasks-1 alternating points in
-    the unit disk and points along a random smooth closed curve (the batched uneven
-    workload), n paths split evenly."""
-    if ntasks <= 1:
-        return precision_point_task(TASK_SEED, "disk"), [n]
-    if n % ntasks:
-        raise SystemExit("--paths must be a multiple of --tasks")
-    tasks = np.stack([precision_point_task(i, "disk" if i % 2 == 0 else "curve") for i in range(ntasks)])
-    return tasks, [n // ntasks] * ntasks
-
-
-def _timed_rounds(torch, tracker, d_fpm, ppt, seeds, outs, depth, world):
-    """K rounds through frg_track_rounds (device buffers, `depth` rounds in flight),
-    bracketed by a barrier and a synchronize on both sides. The library times the
-    span with CUDA events on its launching streams (first launch to the last round's
-    end); torch events on the current stream bracket the call as a cross-check."""
+def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world):
+    """K rounds through frg_track_rounds (device buffers, `depth` rounds in flight, one
+    task set per round), bracketed by a barrier and a synchronize on both sides. The
+    library times the span with CUDA events on its launching streams (first launch to
+    the last round's end); torch events on the current stream bracket the call as a
+    cross-check."""
     roots, codes, resid = outs
     torch.cuda.synchronize()
     if world > 1:
@@ -255,7 +319,7 @@ def _timed_rounds(torch, tracker, d_fpm, ppt, seeds, outs, depth, world):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
-    st = tracker.track_rounds(d_fpm, ppt, seeds, roots, codes, resid=resid, depth=depth)
+    st = tracker.track_rounds(fpm_sets, ppt, seeds, roots, codes, resid=resid, depth=depth, per_round_tasks=True)
     ev1.record()
     torch.cuda.synchronize()
     if world > 1:
@@ -263,57 +327,83 @@ def _timed_rounds(torch, tracker, d_fpm, ppt, seeds, outs, depth, world):
     return st, ev0.elapsed_time(ev1)
 
 
+def _collect(frg, wl, steps, outs, n):
+    """Per-task collections of K steps' device outputs."""
+    R = outs[0].cpu().numpy().view(np.complex128)
+    C = outs[1].cpu().numpy()
+    E = outs[2].cpu().numpy()
+    tc = TaskCollections(lambda: frg.Collection(DUP_TOL), wl.ntasks)
+    for i, s in enumerate(steps):
+        sl = slice(i * n, (i + 1) * n)
+        tc.merge_step(wl, s, R[sl], C[sl], E[sl])
+    return tc
+
+
 def run_ours(args, rank, world):
     import torch
 
     import finite_root_generation_gb300 as frg
     from finite_root_generation_gb300 import build as frg_build
-    from finite_root_generation_gb300.metrics import distinct_roots, recall
-    from finite_root_generation_gb300.tasks import precision_point_task
+    from finite_root_generation_gb300.metrics import recall
 
     frg_build.build()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    task, ppt = workload_tasks(precision_point_task, args.tasks, args.paths)
-    n, k, depth = args.paths, args.steps, args.depth
+    wl = Workload(args.workload)
+    n, k, depth = wl.paths_per_step, args.steps, args.depth
+    ppt = [wl.paths_per_task] * wl.tasks_per_step
     chosen_cfg = workload_config(frg, frg.PREC_MIXED)
-    for key, v in _chosen_overrides().items():
+    for key, v in _chosen_overrides(frg).items():
         setattr(chosen_cfg, key, v)
     chosen = frg.Tracker(chosen_cfg, device=dev)
     plain = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
-    d_fpm = torch.from_numpy(task.view(np.float64).copy()).cuda()
+    # steps of this rank (ranks take disjoint seeds)
+    steps = list(range(k))
+
+    def seed_of(s):
+        return SEED_BASE + 1000 * rank + s
+
+    seeds = [seed_of(s) for s in steps]
+    sets = wl.task_sets(steps)
+    d_sets = torch.from_numpy(sets.view(np.float64).copy()).cuda()
     nbuf = max(k, args.warmup, 1) * n
     outs = (torch.empty((nbuf, 42), dtype=torch.float64, device="cuda"),
             torch.empty(nbuf, dtype=torch.int32, device="cuda"),
             torch.empty(nbuf, dtype=torch.float64, device="cuda"))
-
-    def seed_of(step):
-        return 1000003 * (rank + 1) + step
-
-    seeds = [seed_of(i) for i in range(k)]
-    # warm-up: W rounds of the chosen configuration and one of the plain one
-    warm = [seed_of(-1 - i) for i in range(args.warmup)]
-    chosen.track_rounds(d_fpm, ppt, warm, outs[0][: len(warm) * n], outs[1][: len(warm) * n],
-                        resid=outs[2][: len(warm) * n], depth=depth)
-    plain.track_rounds(d_fpm, [min(c, max(1, 8192 // len(ppt))) for c in ppt], warm[:1], outs[0], outs[1],
-                       resid=outs[2], depth=1)
+    # warm-up: W rounds of the chosen configuration (other seeds) and one small plain round
+    wsteps = list(range(args.warmup))
+    warm = [WARM_SEED_BASE + 1000 * rank + s for s in wsteps]
+    if warm:
+        d_wsets = torch.from_numpy(wl.task_sets(wsteps).view(np.float64).copy()).cuda()
+        chosen.track_rounds(d_wsets, ppt, warm, outs[0][: len(warm) * n], outs[1][: len(warm) * n],
+                            resid=outs[2][: len(warm) * n], depth=depth, per_round_tasks=True)
+        plain.track_rounds(d_wsets[:1], [min(c, 1024) for c in ppt], warm[:1], outs[0], outs[1],
+                           resid=outs[2], depth=1, per_round_tasks=True)
     torch.cuda.synchronize()
 
-    # ---- chosen configuration, inputs resident in HBM (value) ----
+    # ---- chosen configuration, task sets resident in HBM (value) ----
     c_outs = tuple(o[: k * n] for o in outs)
     with ClockSampler(dev) as clk:
-        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_fpm, ppt, seeds, c_outs, depth, world)
+        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_sets, ppt, seeds, c_outs, depth, world)
     clocks = clk.summary()
-    c_sets = _round_sets(*c_outs, n, k)
-    # ---- plain FP64 on the same seeds, pipelined the same way (ratio and recall) ----
-    kp = max(1, min(args.plain_steps, k))
-    p_st, _ = _timed_rounds(torch, plain, d_fpm, ppt, seeds[:kp], tuple(o[: kp * n] for o in outs), depth, world)
-    p_sets = _round_sets(*(o[: kp * n] for o in outs), n, kp)
-    rec = [recall(p_sets[i], c_sets[i]) for i in range(kp)]
+    c_coll = _collect(frg, wl, steps, c_outs, n)
+    # ---- plain FP64 on the same steps, seeds and pipelining (ratio and recall) ----
+    p_st, _ = _timed_rounds(torch, plain, d_sets, ppt, seeds, c_outs, depth, world)
+    p_coll = _collect(frg, wl, steps, c_outs, n)
+    hits = found = 0
+    for t in sorted(p_coll.colls):
+        a = p_coll.roots_of(t)
+        hits += round(recall(a, c_coll.roots_of(t)) * len(a))
+        found += len(a)
+    rec = hits / max(found, 1)
+    # ---- one round of the chosen configuration with nothing else in flight: its FP32 and
+    #      FP64 stages' own durations (the pipelined rounds overlap them) ----
+    solo_st, _ = _timed_rounds(torch, chosen, d_sets[:1], ppt, seeds[:1], tuple(o[:n] for o in outs), 1, world)
 
-    # ---- end to end through the C ABI with pinned host buffers (e2e): per round the
-    #      task upload, tracking, the copy of roots/codes/residuals back, and the host
-    #      duplicate merge of every round ----
+    # ---- end to end through the C ABI with pinned host buffers (e2e): the task upload,
+    #      tracking, the copy of roots/codes/residuals back, and the host duplicate merge
+    #      into the per-task collections ----
+    h_sets = torch.from_numpy(sets.view(np.float64).copy()).pin_memory()
     h_roots = torch.empty((k * n, 42), dtype=torch.float64, pin_memory=True)
     h_codes = torch.empty(k * n, dtype=torch.int32, pin_memory=True)
     h_resid = torch.empty(k * n, dtype=torch.float64, pin_memory=True)
@@ -322,23 +412,28 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    chosen.track_rounds(task, ppt, seeds, hr, hc, resid=he, depth=depth)
+    chosen.track_rounds(h_sets.numpy(), ppt, seeds, hr, hc, resid=he, depth=depth, per_round_tasks=True)
     R = hr.view(np.complex128)
-    e2e_distinct = sum(len(distinct_roots(R[i * n:(i + 1) * n], hc[i * n:(i + 1) * n], he[i * n:(i + 1) * n],
-                                          RESID_MAX)) for i in range(k))
+    e2e_coll = TaskCollections(lambda: frg.Collection(DUP_TOL), wl.ntasks)
+    for i, s in enumerate(steps):
+        sl = slice(i * n, (i + 1) * n)
+        e2e_coll.merge_step(wl, s, R[sl], hc[sl], he[sl])
+    e2e_distinct = e2e_coll.distinct()
     e2e_s = time.perf_counter() - t0
 
     track_ms = c_st["track_ms"]
     p_ms = p_st["track_ms"]
-    distinct = sum(len(d) for d in c_sets)
-    p_distinct = sum(len(d) for d in p_sets)
-    t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct], dtype=torch.float64)
+    distinct = c_coll.distinct()
+    p_distinct = p_coll.distinct()
+    t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct, hits, found],
+                     dtype=torch.float64)
     if world > 1:
         tmax, tsum = t.clone().cuda(), t.clone().cuda()
         torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
         track_ms, e2e_s, p_ms = float(tmax[0]), float(tmax[1]), float(tmax[4])
         distinct, e2e_distinct, p_distinct = float(tsum[2]), float(tsum[3]), float(tsum[5])
+        rec = float(tsum[6]) / max(float(tsum[7]), 1.0)
     chosen_rounds = chosen.config.mixed_rounds
     chosen.close()
     plain.close()
@@ -348,44 +443,46 @@ def run_ours(args, rank, world):
     value = distinct / (track_ms * 1e-3)
     value_plain = p_distinct / (p_ms * 1e-3)
     e2e = e2e_distinct / e2e_s
-    # roofline of each kernel: algorithmic FLOPs of its launches / their CUDA-event time
     peaks = measure_fma_peaks()
     fps = flops_per_solve()
+    # roofline of the whole step: the FMA-pipe time its algorithmic FLOPs need at the two
+    # measured peaks, over the step's time, (F32 / peak32 + F64 / peak64) / T
     solves = c_st["ivp_solves"] + c_st["newton_iters"]
     fp64_solves = c_st["fp64_solves"]
     fp32_solves = solves - fp64_solves
-    ms32 = c_st["stage_ms"][0] / k
-    ms64 = c_st["stage_ms"][1] / k
+    F32, F64 = fp32_solves * fps, fp64_solves * fps
+    T = track_ms * 1e-3
+    frac = (F32 / (peaks["fp32"] * 1e12) + F64 / (peaks["fp64"] * 1e12)) / T
+    # per kernel, from the round with nothing else in flight (non-overlapped stage times)
+    s_solves = solo_st["ivp_solves"] + solo_st["newton_iters"]
+    s64 = solo_st["fp64_solves"]
+    s32 = s_solves - s64
+    ms32, ms64 = solo_st["stage_ms"]
     kernels = {
-        "team_kernel<MODE_LO, float> (FP32 stage)": {
-            "bound": "fp32", "achieved": fp32_solves / k * fps / (ms32 * 1e-3) / 1e12, "peak": peaks["fp32"],
-            "ms_per_launch": ms32, "solves_per_launch": fp32_solves / k},
-        "team_kernel<MODE_RESUME, double> (FP64 stage)": {
-            "bound": "fp64", "achieved": fp64_solves / k * fps / (ms64 * 1e-3) / 1e12, "peak": peaks["fp64"],
-            "ms_per_launch": ms64, "solves_per_launch": fp64_solves / k},
+        "team_kernel<1, float, df> (FP32 stage)": {
+            "bound": "fp32", "achieved": s32 * fps / (ms32 * 1e-3) / 1e12, "peak": peaks["fp32"],
+            "ms_per_launch": ms32, "solves_per_launch": s32},
+        "team_kernel<2, double, double> (FP64 stage)": {
+            "bound": "fp64", "achieved": s64 * fps / (ms64 * 1e-3) / 1e12, "peak": peaks["fp64"],
+            "ms_per_launch": ms64, "solves_per_launch": s64},
     }
     for v in kernels.values():
         v["frac"] = v["achieved"] / v["peak"]
-    dom_name = max(kernels, key=lambda kk: kernels[kk]["ms_per_launch"])
-    dom = kernels[dom_name]
-    p_solves = (p_st["ivp_solves"] + p_st["newton_iters"]) / kp
-    p_ms_round = p_st["stage_ms"][1] / kp
-    plain_roof = p_solves * fps / (p_ms_round * 1e-3) / 1e12
-    h2d = len(ppt) * (16 * 30 + 16 + 8) + 8  # task parameters, gammas, path offsets
-    d2h = n * (16 * 21 + 4 + 8)
+    p_solves = p_st["ivp_solves"] + p_st["newton_iters"]
+    plain_frac = p_solves * fps / (p_ms * 1e-3) / (peaks["fp64"] * 1e12)
+    ntask = wl.tasks_per_step
+    h2d = ntask * (16 * 30 + 16 * 3 + 8) + 8  # task parameters, gammas (3 precisions), path offsets
+    d2h = n * (16 * 21 + 4 + 8) + FRG_COUNTERS_BYTES
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": k,
         "warmup": args.warmup, "ms_per_step": round(track_ms / k, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic (seeded task and start mechanisms)",
-        "config": {"workload": (f"Stephenson II FRG rounds of {n} paths on 1 generic complex precision-point task "
-                                f"(seed {TASK_SEED})" if len(ppt) == 1 else
-                                f"Stephenson II FRG rounds of {n} paths over {len(ppt)} tasks (seeds 0..{len(ppt) - 1}, "
-                                "points in the unit disk / along a random closed curve, alternating)")
-                               + ", complex-normal start mechanisms, random unit gamma per round; "
-                               "FP64 sharpening check, canonical cognates, finite + residual <= 1e-10 checks, "
-                               "duplicate removal",
-                   "paths_per_step": n, "rounds_in_flight": depth,
+        "data": "synthetic (seeded tasks and start mechanisms)",
+        "config": {"workload": wl.describe() + "; complex-normal start mechanisms, random unit gamma per task and "
+                               "round; FP64 sharpening check, canonical cognates, finite + residual <= 1e-10 "
+                               "checks, one duplicate collection per task over the timed steps",
+                   "paths_per_step": n, "tasks_per_step": wl.tasks_per_step, "steps_cover_workload": k >= wl.blocks,
+                   "rounds_in_flight": depth,
                    "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
                              "sharpening included), FP64 team kernel for steps with condition estimate > 1e5 "
                              "(at most 10,000 FP64 solves per path) and for finishing",
@@ -393,104 +490,137 @@ def run_ours(args, rank, world):
                          f"348 B per path: ~{n * 2364 / 1e6:.0f} MB per round, {depth} rounds in flight) exceeds "
                          "the 129 MB L2",
                    "parallelism": f"replicas x{world}"},
-        "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": kp,
-                       "ms_per_step": round(p_ms / kp, 3),
-                       "roofline_frac_fp64": round(plain_roof / peaks["fp64"], 4)},
+        "plain_fp64": {"value": round(value_plain, 2), "unit": UNIT, "steps": k, "rounds_in_flight": depth,
+                       "ms_per_step": round(p_ms / k, 3), "distinct": int(p_distinct),
+                       "roofline_frac_fp64": round(plain_frac, 4)},
         "speedup_vs_plain_fp64": round(value / value_plain, 3),
-        "recall_vs_plain_fp64": round(min(rec), 5),
-        "distinct_roots_per_step": distinct / k / world,
+        "recall_vs_plain_fp64": round(rec, 5),
+        "distinct_roots": int(distinct),
         "torch_event_ms": round(c_torch_ms, 1),
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"kernel": dom_name, "bound": dom["bound"], "achieved": round(dom["achieved"], 4),
-                     "peak": round(dom["peak"], 4), "unit": "TFLOP/s", "frac": round(dom["frac"], 4),
-                     "traffic": None,
-                     "peak_source": "FMA peaks measured live by bench.py (MEASURED_PEAKS.json has no FP32/FP64 "
-                                    "vector figure)",
+        "roofline": {"bound": "fma (fp32 + fp64 pipes)", "achieved": round(frac, 5), "peak": 1.0,
+                     "unit": "fraction of the step's time the algorithmic FLOPs need at the measured FP32 and "
+                             "FP64 FMA peaks: (F32/peak32 + F64/peak64)/T",
+                     "frac": round(frac, 5), "traffic": None,
+                     "f32_tflop": round(F32 / 1e12, 3), "f64_tflop": round(F64 / 1e12, 3),
+                     "peak_fp32_tflops": round(peaks["fp32"], 2), "peak_fp64_tflops": round(peaks["fp64"], 4),
+                     "peak_source": "FMA peaks of measured: bench.py's own chain-free FMA kernels (MEASURED_PEAKS.json "
+                                    "has no FP32/FP64 vector figure)",
                      "flops_per_solve": fps,
-                     "kernels": {kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
-                                 for kk, v in kernels.items()}},
+                     "kernels_one_round_alone": {
+                         kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
+                         for kk, v in kernels.items()}},
         # per round: start values, FP32 and double-float parameter copies, then per mixed
         # round one FP32-stage and one FP64-stage tracking kernel
         "gpu_launches": (3 + 2 * max(1, chosen_rounds)) * k,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args)
+        line["cpu_baseline"] = cpu_baseline(args, wl, steps=[0], paths_per_task=args.cpu_paths)
     return line
 
 
+FRG_COUNTERS_BYTES = 48 * 8
+
+
 # ------------------------------------------------------------------- CPU baseline
-def cpu_baseline(args, sample_paths=None):
-    """The oracle (C restatement of the reference tracker) on all host cores, on the
-    first paths of the same workload."""
+def _gamma_of(uniform01, seed, k):
+    """The random gamma of task k of a call with `seed` (the library's per-task draw:
+    stream 2^64 - 1 - k, index 0)."""
+    phi = 2 * np.pi * uniform01(seed, 2**64 - 1 - k, 0)
+    return complex(np.cos(phi), np.sin(phi))
+
+
+def cpu_baseline(args, wl, steps, paths_per_task, seed_base=SEED_BASE):
+    """The reference tracker on all host cores over a sample of the given steps: for each
+    step, the first `paths_per_task` paths of each of its tasks, with the step's seed,
+    path streams and gammas. Uses the reference's own sources built for the host
+    (oracle/_ref/libfrgref.so, kind "reference") where they were staged, else the oracle's
+    C restatement (kind "port"); duplicates are removed with the same library's merge
+    (SortingDeletingMerging, or the restatement's). Never loads the product library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    import finite_root_generation_gb300 as frg
-    from finite_root_generation_gb300.tasks import precision_point_task
-
-    oracle.build()
-    o = oracle.Oracle()
+    oracle.build(ref=True)
     cores = os.cpu_count() or 1
-    n = sample_paths or args.cpu_sample
-    task = precision_point_task(TASK_SEED, "disk")
-    cfg = o.config(start_dist=1)
-    # random gamma of task 0 as the library draws it (stream 2^64-1, index 0)
-    phi = 2 * np.pi * o.uniform01(1000003, 2**64 - 1, 0)
-    gamma = complex(np.cos(phi), np.sin(phi))
+    use_ref = os.path.exists(oracle.REF_SO)
+    lib = oracle.RefLib() if use_ref else oracle.Oracle()
+    o_cfg = None if use_ref else lib.config(start_dist=1)
+    colls = {}
+    total_paths = 0
     t0 = time.perf_counter()
-    roots, codes, work, yf = o.homotopy_batch(task, gamma, 1000003, np.arange(n), cfg=cfg, nthreads=cores,
-                                             want_yfinal=True)
+    for s in steps:
+        seed = seed_base + s
+        for i, kt in enumerate(wl.step_tasks(s)):
+            fpm = wl.tasks[kt]
+            gamma = _gamma_of(lib.uniform01, seed, i)
+            stream0 = i * wl.paths_per_task
+            if use_ref:
+                roots, codes, yf, resid = lib.homotopy_batch_ex(fpm, gamma, seed, stream0, paths_per_task,
+                                                                start_normal=True, nthreads=cores)
+            else:
+                roots, codes, _, yf = lib.homotopy_batch(fpm, gamma, seed, stream0 + np.arange(paths_per_task),
+                                                         cfg=o_cfg, nthreads=cores, want_yfinal=True)
+                resid = lib.residuals(roots, fpm)
+            zmax = np.max(np.abs(yf[:, :21]), axis=1)
+            finite = np.abs(yf[:, 21]) >= INF_TOL * zmax
+            good = (codes == 0) & finite & (resid <= RESID_MAX)
+            c = np.where(good, 0, 5).astype(np.int32)
+            order = np.argsort(roots[:, 0].real, kind="stable").astype(np.int32)
+            coll = colls.get(kt, np.zeros((0, 21), np.complex128))
+            if use_ref:
+                colls[kt], _ = lib.sort_merge(coll, roots, c, order)
+            else:
+                colls[kt], _ = lib.sort_merge(coll, roots, c, DUP_TOL)
+            total_paths += paths_per_task
     dt = time.perf_counter() - t0
-    # finite check and residual as in the device path
-    zmax = np.max(np.abs(yf[:, :21]), axis=1)
-    inf = (codes == 0) & (np.abs(yf[:, 21]) < INF_TOL * zmax)
-    codes = np.where(inf, 7, codes).astype(np.int32)
-    coll = frg.Collection(1e-6)
-    coll.merge(roots, codes)
-    d = len(coll)
-    return {"value": round(d / dt, 3), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {n} paths of the workload (seed 1000003), {dt:.1f} s on {cores} threads"}
+    d = sum(len(c) for c in colls.values())
+    return {"value": round(d / dt, 3), "unit": UNIT, "cores": cores, "kind": "reference" if use_ref else "port",
+            "distinct": d, "paths": total_paths, "seconds": round(dt, 2),
+            "sample": f"first {paths_per_task} paths of each task of step(s) {steps[0]}..{steps[-1]} "
+                      f"({total_paths} paths, the GPU arm's seeds and path streams), {dt:.1f} s on {cores} threads; "
+                      + ("the reference's own tracker sources built for this host (oracle/_ref/libfrgref.so), "
+                         "duplicates by its SortingDeletingMerging" if use_ref else
+                         "the oracle's C restatement (the reference's sources were not staged)")}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    for _ in range(max(1, args.warmup)):
-        cb = cpu_baseline(args, sample_paths=args.cpu_sample)
-    t0 = time.perf_counter()
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(args, sample_paths=args.cpu_sample)["value"])
-    dt = time.perf_counter() - t0
-    v = float(np.mean(vals))
+    wl = Workload(args.workload)
+    for s in range(args.warmup):
+        cpu_baseline(args, wl, steps=[s], paths_per_task=args.cpu_paths, seed_base=WARM_SEED_BASE)
+    res = cpu_baseline(args, wl, steps=list(range(args.steps)), paths_per_task=args.cpu_paths)
+    v = res["value"]
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tasks and starts)",
-            "config": {"workload": f"Stephenson II FRG round on one precision-point task (seed {TASK_SEED}), "
-                                   "complex-normal starts, random gamma, FP64 + sharpening + dedup",
-                       "paths_per_step": args.cpu_sample, "precision": "plain FP64",
-                       "parallelism": "host threads"},
+            "warmup": args.warmup, "ms_per_step": round(res["seconds"] / args.steps * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded tasks and start mechanisms)",
+            "config": {"workload": wl.describe() + "; complex-normal start mechanisms, random unit gamma per task "
+                                   "and round; FP64 sharpening, canonical cognates, finite + residual <= 1e-10 "
+                                   "checks, one duplicate collection per task over the timed steps",
+                       "paths_per_step": args.cpu_paths * wl.tasks_per_step,
+                       "sample_of_gpu_step": f"first {args.cpu_paths} of each task's {wl.paths_per_task} paths",
+                       "precision": "plain FP64", "parallelism": "host threads"},
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
-                             "sample": cb["sample"] + "; the reference's own sources are not present on the GPU "
-                                       "host, so its C restatement (oracle/frg_oracle.c) is timed"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": res["cores"], "kind": res["kind"],
+                             "sample": res["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--paths", type=int, default=65536)
-    ap.add_argument("--cpu-sample", type=int, default=8192)
-    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--workload", choices=["c5", "c4", "c2"], default="c5")
+    ap.add_argument("--cpu-paths", type=int, default=128, help="CPU arms: paths per task of each sampled step")
     ap.add_argument("--depth", type=int, default=4, help="rounds in flight")
-    ap.add_argument("--tasks", type=int, default=1, help="tasks per round (>1: the batched uneven workload)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 1:
+        raise SystemExit("need --steps >= 1 and --warmup >= 0")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

@@ -125,7 +125,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p]
     lib.frg_track_rounds.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _I64, ctypes.c_int,
-                                     ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(FrgStats)]
     _F = ctypes.POINTER(ctypes.c_float)
     lib.frg_set_mlp.argtypes = [ctypes.c_void_p, _F, _F, _F, ctypes.c_float, ctypes.c_int]
@@ -166,6 +166,20 @@ def default_config(**overrides) -> FrgConfig:
             raise AttributeError(f"frg_config has no field {k}")
         setattr(cfg, k, v)
     return cfg
+
+
+# The chosen mixed-precision setting of the benchmark: FP32 team kernel with double-float
+# points and refinement that also runs the endgame and sharpening, FP64 for steps whose
+# condition estimate exceeds 1e5 and for finishing every root, at most 10,000 FP64 solves
+# per path.
+CHOSEN = dict(precision=PREC_MIXED, mixed_rounds=1, lo_endgame=1, cond_switch=1e5, lo_points=1, fp64_budget=10000)
+
+
+def chosen_config(**overrides) -> FrgConfig:
+    """default_config with the chosen mixed-precision setting (CHOSEN) and `overrides`."""
+    kw = dict(CHOSEN)
+    kw.update(overrides)
+    return default_config(**kw)
 
 
 def _ptr(a) -> int:
@@ -254,14 +268,17 @@ class Tracker:
         self._check(st, "frg_track")
         return stats.as_dict()
 
-    def track_rounds(self, fpm, paths_per_task, seeds, roots, codes, resid=None, depth: int = 2) -> dict:
+    def track_rounds(self, fpm, paths_per_task, seeds, roots, codes, resid=None, depth: int = 2,
+                     per_round_tasks: bool = False) -> dict:
         """Track len(seeds) rounds, up to `depth` in flight (frg_track_rounds); outputs are
-        [rounds * N, ...] buffers, all numpy host arrays or all torch CUDA tensors."""
+        [rounds * N, ...] buffers, all numpy host arrays or all torch CUDA tensors. With
+        per_round_tasks, fpm holds one task set per round ([rounds, ntasks, 30] complex)."""
         ppt = np.ascontiguousarray(np.atleast_1d(np.asarray(paths_per_task, dtype=np.int64)))
         sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
         stats = FrgStats()
         st = self.lib.frg_track_rounds(self._ctx, _ptr(fpm), len(ppt), ppt.ctypes.data_as(_I64), len(sd),
-                                       sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), int(depth), _ptr(roots),
+                                       sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                       1 if per_round_tasks else 0, int(depth), _ptr(roots),
                                        _ptr(codes), _ptr(resid), ctypes.byref(stats))
         self._check(st, "frg_track_rounds")
         return stats.as_dict()

@@ -144,7 +144,7 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   return FRG_OK;
 }
 
-static frg_status check_config(frg_ctx* ctx, const frg_config* c) {
+frg_status frg_check_config(frg_ctx* ctx, const frg_config* c) {
   if (!c) return fail(ctx, FRG_ERR_ARG, "config is NULL");
   if (!(c->s_init > 0) || !(c->s_min > 0) || !(c->s_max >= c->s_min) || !(c->rk_tol > 0))
     return fail(ctx, FRG_ERR_ARG, "step sizes and rk_tol must be positive with s_max >= s_min");
@@ -180,7 +180,7 @@ extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int devic
   frg_config def;
   frg_config_default(&def);
   ctx->cfg = cfg ? *cfg : def;
-  frg_status s = check_config(nullptr, &ctx->cfg);
+  frg_status s = frg_check_config(nullptr, &ctx->cfg);
   if (s != FRG_OK) { delete ctx; return s; }
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
@@ -233,7 +233,7 @@ extern "C" const char* frg_last_error(const frg_ctx* ctx) { return ctx ? ctx->er
 
 extern "C" frg_status frg_set_config(frg_ctx* ctx, const frg_config* cfg) {
   if (!ctx) return FRG_ERR_ARG;
-  frg_status s = check_config(ctx, cfg);
+  frg_status s = frg_check_config(ctx, cfg);
   if (s != FRG_OK) return s;
   ctx->cfg = *cfg;
   return FRG_OK;
@@ -537,12 +537,13 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
 }
 
 extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
-                                       int nrounds, const uint64_t* seeds, int depth, double* roots, int32_t* codes,
-                                       double* resid, frg_stats* stats) {
+                                       int nrounds, const uint64_t* seeds, int per_round_tasks, int depth,
+                                       double* roots, int32_t* codes, double* resid, frg_stats* stats) {
   auto t0 = std::chrono::steady_clock::now();
   if (!ctx) return FRG_ERR_ARG;
   if (nrounds < 1 || !seeds) return fail(ctx, FRG_ERR_ARG, "need nrounds >= 1 and one seed per round");
   if (depth < 1 || depth > 8) return fail(ctx, FRG_ERR_ARG, "depth must be in 1..8");
+  if (per_round_tasks != 0 && per_round_tasks != 1) return fail(ctx, FRG_ERR_ARG, "per_round_tasks must be 0 or 1");
   int64_t N = 0;
   frg_status s = check_track_args(ctx, fpm, ntasks, paths_per_task, roots, codes, &N);
   if (s != FRG_OK) return s;
@@ -560,11 +561,13 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
     sl->own_stream = true;
     ctx->slots.push_back(sl);
   }
-  // the task parameters, once, before any round
+  // the task parameters (one set, or one per round), once, before any round
+  const size_t task_sets = per_round_tasks ? (size_t)nrounds : 1;
   const cx<double>* d_fpm = (const cx<double>*)fpm;
   if (!is_device_ptr(fpm)) {
-    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks));
-    FRG_CUDA(ctx, cudaMemcpy(ctx->fpm.p, fpm, sizeof(cx<double>) * 30 * ntasks, cudaMemcpyHostToDevice));
+    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks * task_sets));
+    FRG_CUDA(ctx, cudaMemcpy(ctx->fpm.p, fpm, sizeof(cx<double>) * FRG_NP * ntasks * task_sets,
+                             cudaMemcpyHostToDevice));
     d_fpm = (const cx<double>*)ctx->fpm.p;
   }
   const bool dev_out = is_device_ptr(roots);
@@ -614,7 +617,8 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
         if (resid) { FRG_CUDA(ctx, sl.resid.ensure(eb)); d_resid = (double*)sl.resid.p; }
       }
       cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
-      s = enqueue_track(ctx, sl, d_fpm, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
+      const cx<double>* fpm_r = d_fpm + (per_round_tasks ? (size_t)r * FRG_NP * ntasks : 0);
+      s = enqueue_track(ctx, sl, fpm_r, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
                         rev);
       if (s != FRG_OK) return s;
       FRG_CUDA(ctx, cudaEventRecord(rev[per], st));

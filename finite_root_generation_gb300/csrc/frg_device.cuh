@@ -21,8 +21,8 @@ constexpr int LDM = 24; // leading dimension of the 23x23 system (+ right-hand s
 
 typedef cx<double> cd;
 
-// Dormand-Prince 6(5) tableau (rungekutta.cu:261-341): stage weights, error
-// weights (LTE, :318-324) and 6th-order solution weights (:334-341).
+// Dormand-Prince 6(5) tableau (rungekutta.cu:40-122): stage weights (:40-95), error
+// weights (LTE, :99-105) and 6th-order solution weights (:115-122).
 static __constant__ double c_dpA[8][7] = {
     {0, 0, 0, 0, 0, 0, 0},
     {1. / 10., 0, 0, 0, 0, 0, 0},

@@ -82,3 +82,6 @@ cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cu
 cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);
 cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream);
+// Validates a run configuration (every field frg_create and frg_set_config accept);
+// ctx may be null, otherwise it receives the error text.
+frg_status frg_check_config(frg_ctx* ctx, const frg_config* c);

@@ -20,6 +20,10 @@
 // before any stream capture. Every call shares the array and it keeps the previous
 // call's contents, so each call first clears the queue head and counters; two calls
 // whose GPU work overlaps (different streams on one device) race on the array.
+//
+// The per-task values (gammas, path counts) reach the array through a small set-up
+// kernel that takes them as a launch parameter, so a call makes no host-to-device
+// copy and reads no host memory after it returns.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -61,13 +65,42 @@ frg_status scratch_on_current_device(NoallocScratch** out) {
   return FRG_OK;
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory that the current device `dev` can use directly; device
+// memory of another GPU is refused.
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes attr;
   if (!p || cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+  if (attr.type == cudaMemoryTypeManaged) return true;
+  return attr.type == cudaMemoryTypeDevice && attr.device == dev;
+}
+
+// Per-task values of one call, passed by value as the set-up kernel's launch
+// parameter (24.6 KB, inside the 32 KB parameter limit of this architecture).
+struct NoallocTasks {
+  int ntasks;
+  int pad;
+  cx<double> gamma[FRG_NOALLOC_MAX_TASKS];
+  int64_t paths[FRG_NOALLOC_MAX_TASKS];
+};
+static_assert(sizeof(NoallocTasks) < 32000, "set-up parameters exceed the kernel parameter limit");
+
+// One block: zero the queue head and counters, copy the gammas, prefix-sum the path
+// counts into task_start.
+__global__ void __launch_bounds__(256) noalloc_setup_kernel(NoallocScratch* sc, const __grid_constant__ NoallocTasks t) {
+  for (int i = threadIdx.x; i < 4; i += blockDim.x) sc->queue[i] = 0ull;
+  for (int i = threadIdx.x; i < FRG_NCOUNTERS; i += blockDim.x) sc->counters[i] = 0ull;
+  for (int k = threadIdx.x; k < t.ntasks; k += blockDim.x) sc->gamma[k] = t.gamma[k];
+  if (threadIdx.x == 0) {
+    int64_t acc = 0;
+    sc->task_start[0] = 0;
+    for (int k = 0; k < t.ntasks; ++k) {
+      acc += t.paths[k];
+      sc->task_start[k + 1] = acc;
+    }
+  }
 }
 
 }  // namespace
@@ -77,39 +110,41 @@ extern "C" frg_status frg_track_noalloc(const frg_config* cfg, const double* fpm
                                         int32_t* codes, double* resid, void* stream) {
   if (!cfg || !fpm || !paths_per_task || ntasks < 1) return FRG_ERR_ARG;
   if (ntasks > FRG_NOALLOC_MAX_TASKS) return FRG_ERR_ARG;  // beyond the static scratch
+  // the same checks as frg_create / frg_set_config (step sizes, iteration limits,
+  // modes), before any GPU work
+  if (frg_check_config(nullptr, cfg) != FRG_OK) return FRG_ERR_ARG;
   if (cfg->precision != FRG_PREC_FP64) return FRG_ERR_ARG;  // mixed precision needs per-path buffers
-  if (cfg->kernel_variant != FRG_KERNEL_TEAM && cfg->kernel_variant != FRG_KERNEL_THREAD) return FRG_ERR_ARG;
-  int64_t starts[FRG_NOALLOC_MAX_TASKS + 1];
-  cx<double> gammas[FRG_NOALLOC_MAX_TASKS];
-  starts[0] = 0;
+  NoallocTasks tk;  // the set-up kernel's launch parameter, built on the host stack
+  NoallocTasks* tp = &tk;
+  tp->ntasks = ntasks;
+  tp->pad = 0;
+  int64_t N = 0;
   for (int k = 0; k < ntasks; ++k) {
     if (paths_per_task[k] < 0) return FRG_ERR_ARG;
-    starts[k + 1] = starts[k] + paths_per_task[k];
+    tp->paths[k] = paths_per_task[k];
+    N += paths_per_task[k];
   }
-  const int64_t N = starts[ntasks];
   if (N == 0) return FRG_OK;
-  if (!roots || !codes || !on_device(fpm) || !on_device(roots) || !on_device(codes) ||
-      (resid && !on_device(resid)))
-    return FRG_ERR_ARG;  // inputs and outputs are the caller's device buffers
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FRG_ERR_CUDA;
+  if (!roots || !codes || !on_device(fpm, dev) || !on_device(roots, dev) || !on_device(codes, dev) ||
+      (resid && !on_device(resid, dev)))
+    return FRG_ERR_ARG;  // inputs and outputs are the caller's buffers on the current device
   for (int k = 0; k < ntasks; ++k) {
     if (cfg->gamma_mode == FRG_GAMMA_FIXED) {
-      gammas[k] = cx<double>(cfg->gamma_re, cfg->gamma_im);
+      tp->gamma[k] = cx<double>(cfg->gamma_re, cfg->gamma_im);
     } else {  // the same per-task draw as frg_track
       const double phi = 6.283185307179586 * frg_uniform01(seed, 0xFFFFFFFFFFFFFFFFull - (uint64_t)k, 0);
-      gammas[k] = cx<double>(std::cos(phi), std::sin(phi));
+      tp->gamma[k] = cx<double>(std::cos(phi), std::sin(phi));
     }
   }
   NoallocScratch* sc = nullptr;
   frg_status s = scratch_on_current_device(&sc);
   if (s != FRG_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
-  // clear what must start at zero; the rest is overwritten
-  if (cudaMemsetAsync(sc, 0, sizeof(sc->queue) + sizeof(sc->counters), st) != cudaSuccess) return FRG_ERR_CUDA;
-  if (cudaMemcpyAsync(sc->gamma, gammas, sizeof(cx<double>) * ntasks, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return FRG_ERR_CUDA;
-  if (cudaMemcpyAsync(sc->task_start, starts, sizeof(int64_t) * (ntasks + 1), cudaMemcpyHostToDevice, st) !=
-      cudaSuccess)
-    return FRG_ERR_CUDA;
+  // clear what must start at zero and fill the per-task values; the rest is overwritten
+  noalloc_setup_kernel<<<1, 256, 0, st>>>(sc, *tp);
+  if (cudaGetLastError() != cudaSuccess) return FRG_ERR_CUDA;
 
   frg::TrackArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -125,9 +160,8 @@ extern "C" frg_status frg_track_noalloc(const frg_config* cfg, const double* fpm
   a.codes = codes;
   a.resid = resid;
   a.counters = sc->counters;
-  int dev = 0, sms = 0, bps = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+  int sms = 0, bps = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return FRG_ERR_CUDA;
   const bool team = cfg->kernel_variant == FRG_KERNEL_TEAM;
   if ((team ? frg_team_occupancy(0, &bps) : frg_track_occupancy(0, &bps)) != cudaSuccess) return FRG_ERR_CUDA;

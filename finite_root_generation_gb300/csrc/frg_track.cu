@@ -66,7 +66,7 @@ __device__ __forceinline__ T vnorm(const cx<T>* v, int n) {
 }
 
 // sum_{l < n} w[l] * s * k[l][e], accumulated from the last term to the first as the
-// reference's nested .add() chains do (rungekutta.cu:262-341).
+// reference's nested .add() chains do (rungekutta.cu:40-122).
 template <typename T>
 __device__ __forceinline__ cx<T> comb(const double* w, T s, const cx<T> (*k)[NY], int n, int e) {
   cx<T> acc(T(0));
@@ -269,7 +269,7 @@ track_kernel(TrackArgs a) {
       for (int e = 0; e < NY; ++e) P.k[P.stage][e] = x[e];
       if (++P.stage == 8) {
         P.stage = 0;
-        // error estimate and step factor (rungekutta.cu:317-331), prediction (:333-341)
+        // error estimate and step factor (rungekutta.cu:99-112), prediction (:115-122)
         T es = T(0);
 #pragma unroll 1
         for (int e = 0; e < NY; ++e) {
@@ -437,7 +437,8 @@ __device__ void finish_path(const TrackArgs& a, int64_t id, int task, int code, 
       double mx = 0.0;
 #pragma unroll 1
       for (int e = 0; e < NZ; ++e) mx = fmax(mx, fmax(fabs(M[i * LDM + e].re), fabs(M[i * LDM + e].im)));
-      r = fmax(r, sqrt(cnorm2(F[i])) / mx);
+      const double ri = sqrt(cnorm2(F[i])) / mx;
+      r = (ri == ri) ? fmax(r, ri) : INFINITY;  // a non-finite row makes the residual infinite
     }
     a.resid[id] = r;
   }

@@ -162,7 +162,9 @@ __device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, i
     for (int c = 0; c < 8; ++c) m0 = fmax(m0, fmax(fabs(o.dI[c].re), fabs(o.dI[c].im)));
     for (int c = 0; c < 6; ++c) m1 = fmax(m1, fmax(fabs(o.dII[c].re), fabs(o.dII[c].im)));
     for (int c = 0; c < 16; ++c) m2 = fmax(m2, fmax(fabs(o.dIII[c].re), fabs(o.dIII[c].im)));
-    double r = fmax(sqrt(cnorm2(o.fI)) / m0, fmax(sqrt(cnorm2(o.fII)) / m1, sqrt(cnorm2(o.fIII)) / m2));
+    const double r0 = sqrt(cnorm2(o.fI)) / m0, r1 = sqrt(cnorm2(o.fII)) / m1, r2 = sqrt(cnorm2(o.fIII)) / m2;
+    // fmax drops NaN operands: a non-finite row makes the residual infinite instead
+    double r = (r0 == r0 && r1 == r1 && r2 == r2) ? fmax(r0, fmax(r1, r2)) : INFINITY;
     r = team_max(tmask, r);
     if (g == 0) a.resid[id] = r;
   }
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     } else if (phase == PH_RK) {
       if (++stage == 8) {
         stage = 0;
-        // error estimate and step factor (rungekutta.cu:317-331), prediction (:333-341)
+        // error estimate and step factor (rungekutta.cu:99-112), prediction (:115-122)
         T es = T(0);
         for (int e = g; e < NY; e += TEAM) {
           cx<T> le = T(c_dpE[7]) * s * S.k[7][e];

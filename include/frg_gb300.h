@@ -178,13 +178,16 @@ frg_status frg_track_async(frg_ctx* ctx, const double* fpm, int ntasks, const in
 /* `nrounds` rounds of the reference driver's loop (frg.cu:351-514, one Homotopy launch
  * per round, seeds[r] in place of its time(NULL) reseed at :359) in one call, pipelined:
  * up to `depth` rounds are in flight on separate streams, so a round's long FP64 tail
- * overlaps the next rounds' tracking. Round r writes roots + r*N*21*2, codes + r*N and
- * resid + r*N (N = sum of paths_per_task); these are all device or all host buffers
- * (host copies are asynchronous when the host memory is pinned). stats sums all rounds;
- * track_ms spans the first launch to the last round's end. */
+ * overlaps the next rounds' tracking. per_round_tasks = 0: every round tracks the same
+ * ntasks tasks (fpm: ntasks x 30 complex), as the reference's loop does; 1: round r
+ * tracks its own task set (fpm: nrounds x ntasks x 30 complex, set r at r*ntasks*30),
+ * e.g. a large batch of tasks split into rounds. Round r writes roots + r*N*21*2,
+ * codes + r*N and resid + r*N (N = sum of paths_per_task); these are all device or all
+ * host buffers (host copies are asynchronous when the host memory is pinned). stats
+ * sums all rounds; track_ms spans the first launch to the last round's end. */
 frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
-                            int nrounds, const uint64_t* seeds, int depth, double* roots, int32_t* codes,
-                            double* resid, frg_stats* stats);
+                            int nrounds, const uint64_t* seeds, int per_round_tasks, int depth, double* roots,
+                            int32_t* codes, double* resid, frg_stats* stats);
 
 /* Early retirement (no counterpart in the reference). A 32 -> 64 -> 64 -> 3 ReLU network
  * (BF16 weights, FP32 sums) scores a path's tracking features every `every` accepted
@@ -229,7 +232,9 @@ frg_status frg_mlp_predict(const float* X, int64_t n, const float* params, float
  * GPU that loads the library until exit, so a call takes at most
  * FRG_NOALLOC_MAX_TASKS tasks (more returns FRG_ERR_ARG). The first call on a device
  * looks up the array's device address; make it before any stream capture. All calls
- * share the array: calls whose GPU work overlaps on one device race. Errors are
+ * share the array: calls whose GPU work overlaps on one device race. cfg is checked
+ * like frg_create's (a config frg_create refuses is refused here), and every buffer
+ * must be device memory of the current device (or managed memory). Errors are
  * reported by the status alone (FRG_ERR_ARG for bad arguments, FRG_ERR_CUDA). */
 #define FRG_NOALLOC_MAX_TASKS 1024
 #define FRG_NOALLOC_SCRATCH_BYTES 32768

@@ -50,10 +50,24 @@ class OrStats(ctypes.Structure):
                 ("newton_calls", ctypes.c_int64)]
 
 
+REF_SRC = os.path.join(REF_DIR, "src")
+
+
+def ref_sources_staged() -> bool:
+    """True when the reference's sources were staged into oracle/_ref/src (git-ignored;
+    `make -C oracle stage REF=<reference checkout>`), so libfrgref.so can be built here."""
+    return os.path.exists(os.path.join(REF_SRC, "htpytrack.cu"))
+
+
+def stage(ref_dir: str) -> None:
+    """Copy the reference sources this build needs from `ref_dir` into oracle/_ref/src."""
+    subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF={ref_dir}"], check=True)
+
+
 def build(ref: bool = False) -> None:
-    """Compile the oracle (and, if asked and the sources exist, the reference) with make."""
+    """Compile the oracle (and, if asked and the staged sources exist, the reference) with make."""
     targets = ["port"]
-    if ref:
+    if ref and ref_sources_staged():
         targets.append("ref")
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
@@ -199,6 +213,20 @@ class Oracle:
                                    work.ctypes.data_as(_I64), ctypes.c_int(nthreads))
         return roots, codes, work, yf
 
+    def residuals(self, roots, q):
+        """Row-scaled residual of the target system at dehomogenized roots (Z0 = 1):
+        per root, max over rows of |F_r| / max_c max(|Re J_rc|, |Im J_rc|)."""
+        roots = _c(roots).reshape(-1, 21)
+        out = np.zeros(len(roots))
+        for i, r in enumerate(roots):
+            Z = np.concatenate([r, [1.0]])
+            f = np.abs(self.fsys(Z, q))
+            J = self.jvar(Z, q)
+            m = np.maximum(np.abs(J.real), np.abs(J.imag)).max(axis=1)
+            q = f / m
+            out[i] = np.inf if np.any(np.isnan(q)) else np.max(q)
+        return out
+
     def sort_merge(self, coll, fpt, codes, tol=1e-6):
         coll = _c(coll).reshape(-1, 21)
         fpt = _c(fpt).reshape(-1, 21)
@@ -286,6 +314,33 @@ class RefLib:
                                     ctypes.c_longlong(n), _p(_c(fpm)), _p(_c([gamma])), _p(roots),
                                     codes.ctypes.data_as(_I), ctypes.c_int(nthreads or os.cpu_count() or 1))
         return roots, codes
+
+    def homotopy_batch_ex(self, fpm, gamma, seed, stream0, n, start_normal=False, nthreads=None,
+                          want_yfinal=True):
+        """ref_homotopy_batch_ex: roots, codes, Yfinal (or None) and residuals of paths
+        stream0 .. stream0 + n - 1, start mechanisms U(-5,5)^2 or complex normal."""
+        roots = np.zeros((n, 21), np.complex128)
+        codes = np.zeros(n, np.int32)
+        yf = np.zeros((n, 23), np.complex128) if want_yfinal else None
+        resid = np.zeros(n, np.float64)
+        self.lib.ref_homotopy_batch_ex(ctypes.c_ulonglong(seed), ctypes.c_ulonglong(stream0), ctypes.c_longlong(n),
+                                       _p(_c(fpm)), _p(_c([gamma])), ctypes.c_int(1 if start_normal else 0),
+                                       _p(roots), codes.ctypes.data_as(_I), _p(yf) if yf is not None else None,
+                                       _p(resid), ctypes.c_int(nthreads or os.cpu_count() or 1))
+        return roots, codes, yf, resid
+
+    def residuals(self, roots, q):
+        """Row-scaled residual at dehomogenized roots with the reference's FSYS and JVAR."""
+        roots = _c(roots).reshape(-1, 21)
+        out = np.zeros(len(roots))
+        self.lib.ref_residuals(_p(roots), ctypes.c_longlong(len(roots)), _p(_c(q)), _p(out))
+        return out
+
+    def uniform01(self, seed, stream, index):
+        f = self.lib.ref_uniform01
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_ulonglong]
+        return f(seed, stream, index)
 
     def sort_merge(self, coll, fpt, codes, order):
         coll = _c(coll).reshape(-1, 21)

@@ -12,6 +12,8 @@
  * Complex arrays are interleaved (re, im) doubles, the byte layout of the
  * reference's Vect<M>/Matr<R,C> (classes.cuh:52-54, 136-139).
  */
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <deque>
 #include <thread>
@@ -190,6 +192,92 @@ void ref_homotopy_batch(unsigned long long seed, unsigned long long stream0, lon
     });
   }
   for (auto& t : pool) t.join();
+}
+
+/* Row-scaled residual of the target system at a dehomogenized root (Z0 = 1):
+   max over the 21 rows of |F_r| / max_c max(|Re J_rc|, |Im J_rc|), with FSYS and JVAR
+   (htpykinematics.cu:8, :129) -- the residual the GPU tracker reports per root. */
+static double root_residual(const Vect<nV>* root, const Vect<nP>* q) {
+  Vect<nV + 1> z; Vect<nP> p = *q; Vect<nV> f; Matr<nV, nV + 1> m;
+  std::memcpy(z.vals, root->vals, sizeof(Cplx) * nV);
+  z.vals[nV] = {1.0, 0.0};
+  FSYS(&z, &p, &f);
+  JVAR(&z, &p, &m);
+  double r = 0.0;
+  for (int i = 0; i < nV; ++i) {
+    double mx = 0.0;
+    for (int c = 0; c < nV + 1; ++c) {
+      const Cplx v = m.vals[i * (nV + 1) + c];
+      mx = std::max(mx, std::max(std::fabs(v.x), std::fabs(v.y)));
+    }
+    const double fr = std::sqrt(f.vals[i].x * f.vals[i].x + f.vals[i].y * f.vals[i].y);
+    const double ri = fr / mx;
+    r = (ri == ri) ? std::max(r, ri) : INFINITY;  /* a non-finite row: infinite residual */
+  }
+  return r;
+}
+
+/* The reference kernel body for one path (frg.cu:41-68) with the start mechanism drawn
+   either as the reference draws it (start_normal = 0: U(-5,5)^2, frgkinematics.cu:7-8)
+   or complex normal (start_normal = 1, through the stub's mode 1); TrackPath gets the
+   fresh state by value as in frg.cu:54,57. Also returns Yfinal (23 complex) and the
+   root's residual. */
+void ref_homotopy_path_ex(unsigned long long seed, unsigned long long stream, const double* fpm,
+                          const double* gamma, int start_normal, double* root, int* code, double* Yfinal_out,
+                          double* resid) {
+  curandState st; curand_init(seed, stream, 0, &st);
+  curandState st_start = st;
+  st_start.mode = start_normal ? 1 : 0;
+  Cplx g = {gamma[0], gamma[1]};
+  Vect<nV + 2> u_dehom;
+  std::memset(u_dehom.vals, 0, sizeof(Vect<nV + 2>));
+  u_dehom.vals[nV] = {1., 0};
+  Vect<nV + 2> Yfinal;
+  Vect<nV>* spt = (Vect<nV>*)&Yfinal;
+  Vect<nP> spm, f;
+  load(&f, fpm);
+  GenerateStart(st_start, spt, &spm);
+  TrackPath(spt, &spm, &f, &g, st, &Yfinal, code);
+  if (Yfinal_out) store(&Yfinal, Yfinal_out);
+  SwitchPatch(&u_dehom, &Yfinal, &Yfinal);
+  Vect<nV> cogn[2];
+  cogn[0].set(Yfinal.vals);
+  CognateSolns(&cogn[0], &f, cogn);
+  store(&cogn[0], root);
+  if (resid) *resid = root_residual(&cogn[0], &f);
+}
+
+/* A batch of ref_homotopy_path_ex on `nthreads` host threads, streams stream0 ..
+   stream0 + n - 1 (yfinal and resid optional). */
+void ref_homotopy_batch_ex(unsigned long long seed, unsigned long long stream0, long long n, const double* fpm,
+                           const double* gamma, int start_normal, double* roots, int* codes, double* yfinal,
+                           double* resid, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  std::vector<std::thread> pool;
+  for (int w = 0; w < nthreads; ++w) {
+    pool.emplace_back([=]() {
+      for (long long i = w; i < n; i += nthreads)
+        ref_homotopy_path_ex(seed, stream0 + (unsigned long long)i, fpm, gamma, start_normal, roots + 2 * nV * i,
+                             codes + i, yfinal ? yfinal + 2 * (nV + 2) * i : nullptr, resid ? resid + i : nullptr);
+    });
+  }
+  for (auto& t : pool) t.join();
+}
+
+/* root_residual for n dehomogenized roots (n x 21 complex) of the target fpm. */
+void ref_residuals(const double* roots, long long n, const double* fpm, double* out) {
+  Vect<nP> f;
+  load(&f, fpm);
+  for (long long i = 0; i < n; ++i) {
+    Vect<nV> r;
+    load(&r, roots + 2 * nV * i);
+    out[i] = root_residual(&r, &f);
+  }
+}
+
+/* One uniform draw of the shared Philox stream (the stub's generator). */
+double ref_uniform01(unsigned long long seed, unsigned long long stream, unsigned long long index) {
+  return frg_uniform01(seed, stream, index);
 }
 
 /* SortingDeletingMerging (frgsupport.cu:10) on a collection held by the caller.

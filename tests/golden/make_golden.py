@@ -1,7 +1,8 @@
 """Record golden vectors from the reference tracker's own sources.
 
-Builds ``oracle/_ref/libfrgref.so`` from the reference sources (``oracle/Makefile``,
-REF=/root/reference by default; the sources are read in place, never copied) and
+Builds ``oracle/_ref/libfrgref.so`` from the reference sources (``oracle/Makefile``:
+the environment variable REF names the reference checkout; ``make stage`` copies its
+sources into the git-ignored ``oracle/_ref/src``, never into tracked files) and
 records, on seeded inputs:
 
 * FSYS / JVAR / JPAR        (htpykinematics.cu:8, :129, :1132)
@@ -16,7 +17,7 @@ records, on seeded inputs:
 * LambertW                  (frgsupport.cu:249)
 
 into ``tests/golden/ref_golden.npz``. Run from the repository root:
-``python tests/golden/make_golden.py``.
+``REF=<reference checkout> python tests/golden/make_golden.py``.
 """
 from __future__ import annotations
 
@@ -41,6 +42,10 @@ def crand(rng, n, r=2.0):
 
 
 def main() -> None:
+    ref_dir = os.environ.get("REF")
+    if not ref_dir:
+        raise SystemExit("set REF to the reference checkout")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "stage", f"REF={ref_dir}"], check=True)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     ref = RefLib()
     rng = np.random.default_rng(20261203)

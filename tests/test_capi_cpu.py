@@ -157,3 +157,10 @@ def test_noalloc_rejects_bad_arguments_without_a_gpu():
     buf = (ctypes.c_double * 8)()
     assert lib.frg_track_noalloc(ctypes.byref(cfg), buf, many, ppt_many, ctypes.c_uint64(1), buf, buf, None,
                                  None) == -1
+    # configurations frg_create refuses are refused before any GPU work (a negative
+    # ministep limit would never end a rejecting path)
+    for bad in (dict(max_ministeps=-1), dict(max_steps=-1), dict(s_min=0.0), dict(rk_tol=0.0),
+                dict(gamma_mode=7), dict(start_dist=3), dict(path_offset=-5), dict(newt_attempts=0)):
+        c = frg.default_config(**bad)
+        assert lib.frg_track_noalloc(ctypes.byref(c), buf, 1, ppt, ctypes.c_uint64(1), buf, buf, None,
+                                     None) == -1, bad

@@ -50,3 +50,22 @@ def test_rounds_device_buffers():
     got = d_roots.cpu().numpy().view(np.complex128)
     assert np.array_equal(d_codes.cpu().numpy(), np.concatenate([r.codes for r in ref]))
     assert np.array_equal(got, np.concatenate([r.roots for r in ref]))
+
+
+def test_rounds_per_round_task_sets():
+    """Each round tracks its own task set (a batch of tasks split into rounds): the same
+    results as one frg_track call per round on that round's tasks."""
+    frg_build.build()
+    sets = np.stack([np.stack([precision_point_task(8 * r + k, "disk" if k % 2 == 0 else "curve")
+                               for k in range(2)]) for r in range(3)])
+    ppt, seeds = [256, 256], [21, 22, 23]
+    n = sum(ppt)
+    with frg.Tracker(_cfg(frg.PREC_MIXED)) as t:
+        single = [t.track(sets[r], ppt, sd, want_resid=True) for r, sd in enumerate(seeds)]
+        roots = np.zeros((len(seeds) * n, 21), np.complex128)
+        codes = np.zeros(len(seeds) * n, np.int32)
+        resid = np.zeros(len(seeds) * n, np.float64)
+        t.track_rounds(sets, ppt, seeds, roots, codes, resid=resid, depth=2, per_round_tasks=True)
+    assert np.array_equal(codes, np.concatenate([r.codes for r in single]))
+    assert np.array_equal(roots, np.concatenate([r.roots for r in single]))
+    assert np.array_equal(resid, np.concatenate([r.resid for r in single]))
