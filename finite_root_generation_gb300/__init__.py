@@ -61,6 +61,7 @@ class FrgConfig(ctypes.Structure):
         ("mixed_rounds", ctypes.c_int), ("lo_refine", ctypes.c_int), ("lo_endgame", ctypes.c_int),
         ("path_offset", ctypes.c_int64), ("fp64_budget", ctypes.c_int), ("lo_points", ctypes.c_int),
         ("fp64_segment", ctypes.c_int), ("handback_good", ctypes.c_int), ("lo_final", ctypes.c_int),
+        ("carry_handback", ctypes.c_int), ("round_graph", ctypes.c_int),
     ]
 
 

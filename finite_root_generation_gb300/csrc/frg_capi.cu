@@ -83,6 +83,10 @@ struct frg_ctx {
   int last_rounds = 0;
   unsigned long long* h_counters = nullptr;  // pinned per-round counter copies (frg_track_rounds)
   size_t h_counters_n = 0;
+  // call-wide buffers of frg_track_rounds with carry_handback: every round's task sets,
+  // gammas and seeds, one hand-off record per path of the call, output staging
+  DevBuf c_fpm, c_fpm_lo, c_fpm_df, c_gamma, c_gamma_lo, c_gamma_df, c_seeds, c_task_start, c_rec, c_roots,
+      c_codes, c_resid;
   // early-retirement network (frg_set_mlp) and checkpoint features (frg_track_features)
   DevBuf mlp_w, mlp_norm, feat, nfeat;
   float mlp_threshold = 1.f;
@@ -141,6 +145,8 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->fp64_segment = 96;
   c->handback_good = 16;
   c->lo_final = 0;
+  c->carry_handback = 0;
+  c->round_graph = 0;
   return FRG_OK;
 }
 
@@ -165,6 +171,8 @@ frg_status frg_check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->lo_refine < 0 || c->lo_refine > 2) return fail(ctx, FRG_ERR_ARG, "lo_refine must be 0, 1 or 2");
   if (c->lo_points < 0 || c->lo_points > 1) return fail(ctx, FRG_ERR_ARG, "lo_points must be 0 or 1");
   if (c->lo_final < 0 || c->lo_final > 1) return fail(ctx, FRG_ERR_ARG, "lo_final must be 0 or 1");
+  if (c->carry_handback < 0 || c->carry_handback > 1) return fail(ctx, FRG_ERR_ARG, "carry_handback must be 0 or 1");
+  if (c->round_graph < 0 || c->round_graph > 1) return fail(ctx, FRG_ERR_ARG, "round_graph must be 0 or 1");
   if (c->fp64_segment < 0 || c->handback_good < 0)
     return fail(ctx, FRG_ERR_ARG, "fp64_segment and handback_good must be non-negative");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
@@ -219,7 +227,9 @@ extern "C" void frg_destroy(frg_ctx* ctx) {
     delete sl;
   }
   for (DevBuf* b : {&ctx->fpm, &ctx->roots, &ctx->codes, &ctx->yfinal, &ctx->resid, &ctx->mlp_w, &ctx->mlp_norm,
-                    &ctx->feat, &ctx->nfeat})
+                    &ctx->feat, &ctx->nfeat, &ctx->c_fpm, &ctx->c_fpm_lo, &ctx->c_fpm_df, &ctx->c_gamma,
+                    &ctx->c_gamma_lo, &ctx->c_gamma_df, &ctx->c_seeds, &ctx->c_task_start, &ctx->c_rec, &ctx->c_roots,
+                    &ctx->c_codes, &ctx->c_resid})
     b->release();
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -536,6 +546,204 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
   return FRG_OK;
 }
 
+// frg_track_rounds with carry_handback: round r runs on slot r % depth; its FP64 launch
+// hands paths that are well conditioned again to the FP32 launch of round r + depth (the
+// next round on the same stream), which takes them before its fresh paths. Paths are
+// addressed by their global index r * N + i, so records, lists and outputs are call-wide;
+// the last `depth` rounds' FP64 launches finish every path they hold. d_fpm holds one
+// task set (shared) or nrounds sets; outputs are device buffers of nrounds * N paths.
+// evs: per round (per + 1) events, then one more for the end of the uploads. With
+// round_graph the rounds of all streams are captured into one CUDA graph (the streams
+// fork from and join into slot 0's stream), launched once, and this function returns
+// after it finished.
+static frg_status enqueue_rounds_carry(frg_ctx* ctx, const cx<double>* d_fpm, bool per_round_tasks, int ntasks,
+                                       const int64_t* ppt, int nrounds, const uint64_t* seeds, int depth, int64_t N,
+                                       cx<double>* d_roots, int32_t* d_codes, double* d_resid,
+                                       std::vector<cudaEvent_t>& evs, int per) {
+  const size_t K = (size_t)nrounds, T = (size_t)ntasks, KN = K * (size_t)N;
+  cudaStream_t st0 = ctx->slots[0]->stream;
+  // every round's task set (replicated when shared) in FP64, FP32 and double-float
+  FRG_CUDA(ctx, ctx->c_fpm.ensure(sizeof(cx<double>) * FRG_NP * T * K));
+  FRG_CUDA(ctx, ctx->c_fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * T * K));
+  FRG_CUDA(ctx, ctx->c_fpm_df.ensure(sizeof(cx<df>) * FRG_NP * T * K));
+  cx<double>* c_fpm = (cx<double>*)ctx->c_fpm.p;
+  const size_t set_bytes = sizeof(cx<double>) * FRG_NP * T;
+  if (per_round_tasks) {
+    FRG_CUDA(ctx, cudaMemcpyAsync(c_fpm, d_fpm, set_bytes * K, cudaMemcpyDeviceToDevice, st0));
+  } else {
+    for (size_t r = 0; r < K; ++r)
+      FRG_CUDA(ctx, cudaMemcpyAsync((char*)c_fpm + set_bytes * r, d_fpm, set_bytes, cudaMemcpyDeviceToDevice, st0));
+  }
+  FRG_CUDA(ctx, frg_launch_to_float(c_fpm, (cx<float>*)ctx->c_fpm_lo.p, (int)(FRG_NP * T * K), st0));
+  FRG_CUDA(ctx, frg_launch_to_df(c_fpm, (cx<df>*)ctx->c_fpm_df.p, (int)(FRG_NP * T * K), st0));
+  // gammas of every round (the same per-round draw as frg_track), seeds, path offsets
+  std::vector<cx<double>> g_all(T * K);
+  std::vector<cx<float>> g_lo(T * K);
+  std::vector<cx<df>> g_df(T * K);
+  for (size_t r = 0; r < K; ++r) {
+    std::vector<cx<double>> g;
+    task_gammas(ctx->cfg, seeds[r], ntasks, g);
+    for (size_t k = 0; k < T; ++k) {
+      g_all[r * T + k] = g[k];
+      g_lo[r * T + k] = cx<float>(g[k]);
+      g_df[r * T + k] = cx<df>(df(g[k].re), df(g[k].im));
+    }
+  }
+  std::vector<int64_t> starts(T + 1, 0);
+  for (size_t k = 0; k < T; ++k) starts[k + 1] = starts[k] + ppt[k];
+  FRG_CUDA(ctx, ctx->c_gamma.ensure(sizeof(cx<double>) * T * K));
+  FRG_CUDA(ctx, ctx->c_gamma_lo.ensure(sizeof(cx<float>) * T * K));
+  FRG_CUDA(ctx, ctx->c_gamma_df.ensure(sizeof(cx<df>) * T * K));
+  FRG_CUDA(ctx, ctx->c_seeds.ensure(sizeof(uint64_t) * K));
+  FRG_CUDA(ctx, ctx->c_task_start.ensure(sizeof(int64_t) * (T + 1)));
+  FRG_CUDA(ctx, ctx->c_rec.ensure(sizeof(frg::Handoff) * KN));
+  // per-slot lists: [0] FP64 queue of a round, [1 + p] paths carried between the slot's
+  // rounds (p alternates); each holds at most every path of the call
+  for (int d = 0; d < depth; ++d) {
+    Slot& sl = *ctx->slots[d];
+    FRG_CUDA(ctx, sl.lo_lists.ensure(sizeof(int64_t) * 3 * KN));
+    FRG_CUDA(ctx, sl.queue.ensure(sizeof(unsigned long long) * 8));
+    FRG_CUDA(ctx, sl.counters.ensure(sizeof(unsigned long long) * FRG_NCOUNTERS));
+    FRG_CUDA(ctx, sl.starts.ensure(sizeof(cx<double>) * frg::FRG_START_STRIDE * (size_t)N));
+  }
+  // synchronous uploads: the host vectors go out of scope when this function returns
+  FRG_CUDA(ctx, cudaStreamSynchronize(st0));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->c_gamma.p, g_all.data(), sizeof(cx<double>) * T * K, cudaMemcpyHostToDevice));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->c_gamma_lo.p, g_lo.data(), sizeof(cx<float>) * T * K, cudaMemcpyHostToDevice));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->c_gamma_df.p, g_df.data(), sizeof(cx<df>) * T * K, cudaMemcpyHostToDevice));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->c_seeds.p, seeds, sizeof(uint64_t) * K, cudaMemcpyHostToDevice));
+  FRG_CUDA(ctx, cudaMemcpy(ctx->c_task_start.p, starts.data(), sizeof(int64_t) * (T + 1), cudaMemcpyHostToDevice));
+  cudaEvent_t ev_ready = evs.back();
+  FRG_CUDA(ctx, cudaEventRecord(ev_ready, st0));
+  for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, ev_ready, 0));
+
+  const bool graph = ctx->cfg.round_graph != 0;
+  cudaGraph_t g_graph = nullptr;
+  cudaGraphExec_t g_exec = nullptr;
+  std::vector<cudaEvent_t> fj;  // fork and join events of the capture
+  struct GraphGuard {
+    cudaGraph_t& g;
+    cudaGraphExec_t& x;
+    std::vector<cudaEvent_t>& ev;
+    ~GraphGuard() {
+      if (x) cudaGraphExecDestroy(x);
+      if (g) cudaGraphDestroy(g);
+      for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+  } gguard{g_graph, g_exec, fj};
+  if (graph) {
+    frg_status fs = ensure_events(ctx, fj, (size_t)depth + 1);
+    if (fs != FRG_OK) return fs;
+    FRG_CUDA(ctx, cudaStreamBeginCapture(st0, cudaStreamCaptureModeRelaxed));
+    FRG_CUDA(ctx, cudaEventRecord(fj[0], st0));
+    for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, fj[0], 0));
+  }
+  // timing events: event-record nodes when captured
+  auto record = [&](cudaEvent_t ev, cudaStream_t st) {
+    return graph ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
+  };
+
+  frg::TrackArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.cfg = ctx->cfg;
+  a.fpm = c_fpm;
+  a.gamma = (const cx<double>*)ctx->c_gamma.p;
+  a.fpm_lo = (const cx<float>*)ctx->c_fpm_lo.p;
+  a.gamma_lo = (const cx<float>*)ctx->c_gamma_lo.p;
+  a.fpm_df = (const cx<df>*)ctx->c_fpm_df.p;
+  a.gamma_df = (const cx<df>*)ctx->c_gamma_df.p;
+  a.task_start = (const int64_t*)ctx->c_task_start.p;
+  a.ntasks = ntasks;
+  a.npaths = N;
+  a.seeds = (const uint64_t*)ctx->c_seeds.p;
+  a.roots = d_roots;
+  a.codes = d_codes;
+  a.resid = d_resid;
+  a.handoff = (frg::Handoff*)ctx->c_rec.p;
+  auto grid_for = [&](int mode) {
+    int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm : ctx->team_blocks_per_sm[mode];
+    int64_t grid = (int64_t)ctx->sm_count * bps;
+    return (int)(grid < 1 ? 1 : grid);
+  };
+  const int lo_mode = ctx->cfg.lo_points == 1 ? 3 : 1;
+  auto rounds = [&]() -> frg_status {
+    for (int r = 0; r < nrounds; ++r) {
+      Slot& sl = *ctx->slots[r % depth];
+      cudaStream_t st = sl.stream;
+      cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
+      int64_t* lists = (int64_t*)sl.lo_lists.p;
+      unsigned long long* q = (unsigned long long*)sl.queue.p;
+      const int pout = (r / depth) & 1, pin = pout ^ 1;
+      const bool has_in = r >= depth;
+      // queue heads and this round's FP64-list count; the carried-in count (written by
+      // this slot's previous FP64 launch) is kept
+      FRG_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned long long) * 3, st));
+      FRG_CUDA(ctx, cudaMemsetAsync(q + 3 + pout, 0, sizeof(unsigned long long), st));
+      if (!has_in) FRG_CUDA(ctx, cudaMemsetAsync(q + 3 + pin, 0, sizeof(unsigned long long), st));
+      FRG_CUDA(ctx, cudaMemsetAsync(sl.counters.p, 0, sizeof(unsigned long long) * FRG_NCOUNTERS, st));
+      a.seed = seeds[r];
+      a.round_base = (int64_t)r * N;
+      a.counters = (unsigned long long*)sl.counters.p;
+      a.starts = (const cx<double>*)sl.starts.p;
+      {  // start values of this round's fresh paths (task set r)
+        frg::TrackArgs sa = a;
+        sa.fpm = c_fpm + (size_t)r * FRG_NP * T;
+        cudaError_t e = frg_launch_starts(sa, (cx<double>*)sl.starts.p, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "start kernel launch");
+      }
+      FRG_CUDA(ctx, record(rev[0], st));
+      // FP32 stage: carried paths, then this round's fresh paths
+      a.queue = q;
+      a.carry = 1;
+      a.lo_list = has_in ? lists + (size_t)(1 + pin) * KN : nullptr;
+      a.lo_count = has_in ? q + 3 + pin : nullptr;
+      a.handoff_list = lists;
+      a.handoff_count = q + 2;
+      a.back_list = nullptr;
+      a.back_count = nullptr;
+      a.lo_keep_ill = 0;
+      cudaError_t e = frg_launch_team(lo_mode, a, grid_for(lo_mode), st);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP32 stage)");
+      FRG_CUDA(ctx, record(rev[1], st));
+      // FP64 stage: hand well-conditioned paths to round r + depth, or finish them all
+      a.queue = q + 1;
+      a.carry = 0;
+      a.lo_list = nullptr;
+      a.lo_count = nullptr;
+      a.back_list = (r + depth < nrounds) ? lists + (size_t)(1 + pout) * KN : nullptr;
+      a.back_count = q + 3 + pout;
+      e = frg_launch_team(2, a, grid_for(2), st);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "track kernel launch (FP64 stage)");
+      FRG_CUDA(ctx, record(rev[2], st));
+      FRG_CUDA(ctx, record(rev[per], st));
+      FRG_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters + (size_t)r * FRG_NCOUNTERS, sl.counters.p,
+                                    sizeof(unsigned long long) * FRG_NCOUNTERS, cudaMemcpyDeviceToHost, st));
+    }
+    return FRG_OK;
+  };
+  frg_status rs = rounds();
+  if (rs != FRG_OK) {
+    if (graph) {  // leave capture mode; the partial graph is discarded
+      cudaGraph_t partial = nullptr;
+      cudaStreamEndCapture(st0, &partial);
+      if (partial) cudaGraphDestroy(partial);
+      cudaGetLastError();
+    }
+    return rs;
+  }
+  if (graph) {
+    for (int d = 1; d < depth; ++d) {
+      FRG_CUDA(ctx, cudaEventRecord(fj[d], ctx->slots[d]->stream));
+      FRG_CUDA(ctx, cudaStreamWaitEvent(st0, fj[d], 0));
+    }
+    FRG_CUDA(ctx, cudaStreamEndCapture(st0, &g_graph));
+    FRG_CUDA(ctx, cudaGraphInstantiate(&g_exec, g_graph, 0));
+    FRG_CUDA(ctx, cudaGraphLaunch(g_exec, st0));
+    FRG_CUDA(ctx, cudaStreamSynchronize(st0));
+  }
+  return FRG_OK;
+}
+
 extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntasks, const int64_t* paths_per_task,
                                        int nrounds, const uint64_t* seeds, int per_round_tasks, int depth,
                                        double* roots, int32_t* codes, double* resid, frg_stats* stats) {
@@ -596,6 +804,40 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
   for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, ev_start, 0));
   const size_t rb = sizeof(cx<double>) * 21 * (size_t)N, cb = sizeof(int32_t) * (size_t)N,
                eb = sizeof(double) * (size_t)N;
+  const bool carry = mixed && ctx->cfg.carry_handback && ctx->cfg.kernel_variant == FRG_KERNEL_TEAM && mr == 1;
+  if (carry) {
+    // outputs: the caller's device buffers, or call-wide staging copied back at the end
+    // (a round's paths may finish in a later round's launches)
+    cx<double>* d_roots = (cx<double>*)roots;
+    int32_t* d_codes = codes;
+    double* d_resid = resid;
+    if (!dev_out) {
+      FRG_CUDA(ctx, ctx->c_roots.ensure(rb * nrounds));
+      FRG_CUDA(ctx, ctx->c_codes.ensure(cb * nrounds));
+      d_roots = (cx<double>*)ctx->c_roots.p;
+      d_codes = (int32_t*)ctx->c_codes.p;
+      if (resid) { FRG_CUDA(ctx, ctx->c_resid.ensure(eb * nrounds)); d_resid = (double*)ctx->c_resid.p; }
+    }
+    std::vector<cudaEvent_t> cev;
+    s = ensure_events(ctx, cev, 1);
+    if (s != FRG_OK) return s;
+    struct CevGuard {
+      std::vector<cudaEvent_t>& v;
+      ~CevGuard() { for (cudaEvent_t e : v) cudaEventDestroy(e); }
+    } cguard{cev};
+    std::vector<cudaEvent_t> evs_c(evs.begin(), evs.end() - 1);
+    evs_c.push_back(cev[0]);
+    s = enqueue_rounds_carry(ctx, d_fpm, per_round_tasks != 0, ntasks, paths_per_task, nrounds, seeds, depth, N,
+                             d_roots, d_codes, d_resid, evs_c, per);
+    for (int d = 0; d < depth; ++d) cudaStreamSynchronize(ctx->slots[d]->stream);
+    if (s != FRG_OK) return s;
+    FRG_CUDA(ctx, cudaGetLastError());
+    if (!dev_out) {
+      FRG_CUDA(ctx, cudaMemcpy(roots, d_roots, rb * nrounds, cudaMemcpyDeviceToHost));
+      FRG_CUDA(ctx, cudaMemcpy(codes, d_codes, cb * nrounds, cudaMemcpyDeviceToHost));
+      if (resid) FRG_CUDA(ctx, cudaMemcpy(resid, d_resid, eb * nrounds, cudaMemcpyDeviceToHost));
+    }
+  } else {
   // on a failure part-way, rounds already enqueued must finish before the caller's
   // buffers can be reused: drain every slot's stream, then report the first error
   auto enqueue_all = [&]() -> frg_status {
@@ -638,6 +880,7 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
     return s;
   }
   for (int d = 0; d < depth; ++d) FRG_CUDA(ctx, cudaStreamSynchronize(ctx->slots[d]->stream));
+  }
   if (stats) {
     float span = 0.f;
     for (int r = 0; r < nrounds; ++r) {

@@ -45,8 +45,16 @@ struct TrackArgs {
   const cx<df>* gamma_df;
   const int64_t* task_start;    // ntasks + 1 prefix sums of paths per task
   int ntasks;
-  int64_t npaths;
+  int64_t npaths;               // paths of one round
   uint64_t seed;
+  // Paths are addressed by a global index gid = round * npaths + (index within the round):
+  // records, lists and outputs use gid; the random stream, start values and task use the
+  // index within the round; task parameters and gammas are indexed by round * ntasks + task.
+  // A single call is round 0 (gid = index within the round).
+  int64_t round_base;           // gid of this launch's first fresh path (round * npaths)
+  const uint64_t* seeds;        // per-round seeds (null: every path uses `seed`)
+  int carry;                    // FP32 stage: lo_list holds paths carried over from an earlier
+                                // round's FP64 launch, taken before this round's fresh paths
   unsigned long long* queue;    // work-queue head, zeroed before launch
   cx<double>* roots;            // npaths x 21
   int32_t* codes;               // npaths

@@ -110,10 +110,11 @@ template <> __device__ __forceinline__ cx<float> gamma_of<float>(const TrackArgs
 
 // Finish a path (FP64, spread over the team): finite check, dehomogenize
 // (frg.cu:44-46, :60), canonical cognate (frgkinematics.cu:227-285, frg.cu:63-65), the
-// row-scaled residual of the target system at the root, outputs and counters.
-__device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, int64_t id, int task, int code,
+// row-scaled residual of the target system at the root, outputs and counters. id is the
+// path's global index, ti its task-set index.
+__device__ void team_finish(const TrackArgs& a, Smem<double>& S, const cd* Yf, int64_t id, int ti, int code,
                             int g, unsigned tmask, int n_ivp, int n_newton, int steps) {
-  const cd* fpm = a.fpm + (size_t)task * NP;
+  const cd* fpm = a.fpm + (size_t)ti * NP;
   if (a.yfinal)
     for (int e = g; e < NY; e += TEAM) a.yfinal[(size_t)id * NY + e] = Yf[e];
   double zl = 0.0;
@@ -279,9 +280,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   const int jg = g < 7 ? g + 1 : 7;
   // what this launch works through: fresh paths, paths resumed in FP32 (lo_list),
   // or paths handed to FP64 (handoff_list)
-  const bool lo_resume = LO && a.lo_list != nullptr;
+  const bool lo_resume = LO && a.lo_list != nullptr && !a.carry;
+  const int64_t ncarry = (LO && a.carry && a.lo_list != nullptr) ? (int64_t)*a.lo_count : 0;
   const int64_t nqueue = (MODE == MODE_RESUME) ? (int64_t)*a.handoff_count
-                         : (lo_resume ? (int64_t)*a.lo_count : a.npaths);
+                         : (lo_resume ? (int64_t)*a.lo_count : ncarry + a.npaths);
   // A path returns from FP64 to the next round's FP32 kernel after handback_good
   // consecutive well-conditioned solves, or after fp64_segment FP64 solves in this launch
   // (FP64 latency per solve is high on this part, so long FP64 segments set a launch's
@@ -291,8 +293,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   constexpr int kMaxBounces = 64;
 
   LaneParams<T> lp;
-  int64_t id = -1;
-  int task = 0;
+  int64_t id = -1;      // global path index: records, lists, outputs
+  int64_t lid = 0;      // index within the path's round: random stream, start values, task
+  int ti = 0;           // task-set index (round * ntasks + task): parameters, gamma
+  uint64_t pseed = a.seed;
   T s = T(0), err = T(0), scale = T(0), residual = T(100);
   int tstepQ = 0, streak = 0, step = 0, ministep = 0, stage = 0, attempt = 0, it = 0, code = 0;
   int n_ivp = 0, n_newton = 0;
@@ -318,33 +322,42 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       if (g == 0) qi = atomicAdd(a.queue, 1ull);
       qi = __shfl_sync(tmask, qi, 0, TEAM);
       if ((int64_t)qi >= nqueue) { phase = PH_IDLE; break; }
-      id = (MODE == MODE_RESUME) ? a.handoff_list[qi] : (lo_resume ? a.lo_list[qi] : (int64_t)qi);
+      const bool carried = (int64_t)qi < ncarry;
+      id = (MODE == MODE_RESUME) ? a.handoff_list[qi]
+           : (lo_resume || carried) ? a.lo_list[qi] : a.round_base + ((int64_t)qi - ncarry);
+      const bool resumed = MODE == MODE_RESUME || lo_resume || carried;
+      const int64_t round = id / a.npaths;
+      lid = id - round * a.npaths;
+      pseed = a.seeds ? a.seeds[round] : a.seed;
       int lo = 0, hi = a.ntasks - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (a.task_start[mid] <= id) lo = mid; else hi = mid - 1;
+        if (a.task_start[mid] <= lid) lo = mid; else hi = mid - 1;
       }
-      task = lo;
+      ti = (int)(round * a.ntasks) + lo;
       {
         cd z[14], Uj, sp[6];
-        if (a.starts) {  // precomputed by the start kernel: lane g reads what team_start gives it
-          const cd* st = a.starts + (size_t)id * FRG_START_STRIDE;
+        // start values precomputed by the start kernel hold this launch's round only; a
+        // path of an earlier round (carried over) regenerates them (the same code, the
+        // same values)
+        if (a.starts && round * a.npaths == a.round_base) {
+          const cd* st = a.starts + (size_t)lid * FRG_START_STRIDE;
           for (int e = g; e < 14; e += TEAM) z[e] = st[e];
           Uj = st[13 + jg];
 #pragma unroll
           for (int i = 0; i < 6; ++i) sp[i] = st[21 + param_index(i, jg)];
         } else {
-          team_start(a.seed, (uint64_t)(id + c.path_offset), c.start_dist, c.start_range, jg, z, Uj, sp);
+          team_start(pseed, (uint64_t)(lid + c.path_offset), c.start_dist, c.start_range, jg, z, Uj, sp);
         }
-        const cx<T>* fpmT = fpm_of<T>(a, task);
+        const cx<T>* fpmT = fpm_of<T>(a, ti);
 #pragma unroll
         for (int i = 0; i < 6; ++i) { lp.sp[i] = cx<T>(sp[i]); lp.fp[i] = fpmT[param_index(i, jg)]; }
-        lp.gamma = gamma_of<T>(a, task);
+        lp.gamma = gamma_of<T>(a, ti);
         if (g < 7) {
           S.spm[jg] = cp(sp[2]); S.spm[8 + jg] = cp(sp[3]); S.spm[15 + jg] = cp(sp[4]); S.spm[22 + jg] = cp(sp[5]);
         }
         if (g == 0) { S.spm[0] = cp(sp[0]); S.spm[8] = cp(sp[1]); }
-        if (MODE != MODE_RESUME && !lo_resume) {
+        if (!resumed) {
           for (int e = g; e < 14; e += TEAM) S.Yc[e] = cp(z[e]);
           if (g < 7) S.Yc[13 + jg] = cp(Uj);
           if (g == 7) { S.Yc[21] = cp(P(1)); S.Yc[22] = cp(P(0)); }
@@ -353,7 +366,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
       code = 0; stage = 0; attempt = 0; it = 0; residual = T(100); err = T(0); scale = T(0);
       good = 0; bounces = 0; seg = 0;
       if (g == 0) { S.ck_t[0] = S.ck_t[1] = 0.0; S.ck_s[0] = S.ck_s[1] = 0.f; S.ck_rmax = 0.f; }
-      if (MODE == MODE_RESUME || lo_resume) {
+      if (resumed) {
         const Handoff& h = a.handoff[id];
         for (int e = g; e < NY; e += TEAM) {
           S.Yc[e] = cp(h.Yc[e]); S.Vc[e] = cx<T>(h.Vc[e]); S.u[e] = cx<T>(h.u[e]);
@@ -365,7 +378,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
           if constexpr (!LO) {
             cd Yf[NY];
             for (int e = 0; e < NY; ++e) Yf[e] = h.Yc[e];
-            team_finish(a, *reinterpret_cast<Smem<double>*>(&S), Yf, id, task, h.code, g, tmask, n_ivp, n_newton,
+            team_finish(a, *reinterpret_cast<Smem<double>*>(&S), Yf, id, ti, h.code, g, tmask, n_ivp, n_newton,
                         step);
           }
           continue;  // next path
@@ -376,12 +389,12 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         // TrackPath's patches start at draw 0 of the path's stream (by-value state,
         // frg.cu:54,57); u (htpytrack.cu:53-58) then the random velocity patch (:63-67).
         const double R = c.patch_range;
-        const uint64_t stream = (uint64_t)(id + c.path_offset);
+        const uint64_t stream = (uint64_t)(lid + c.path_offset);
         for (int e = g; e < NY; e += TEAM) {
-          S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, 2 * e) - R),
-                         T(2.0 * R * frg_uniform01(a.seed, stream, 2 * e + 1) - R));
-          S.Vc[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, 46 + 2 * e) - R),
-                          T(2.0 * R * frg_uniform01(a.seed, stream, 47 + 2 * e) - R));
+          S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(pseed, stream, 2 * e) - R),
+                         T(2.0 * R * frg_uniform01(pseed, stream, 2 * e + 1) - R));
+          S.Vc[e] = cx<T>(T(2.0 * R * frg_uniform01(pseed, stream, 46 + 2 * e) - R),
+                          T(2.0 * R * frg_uniform01(pseed, stream, 47 + 2 * e) - R));
         }
         rng_index = 92;
         __syncwarp(tmask);
@@ -430,8 +443,8 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     long long tc2 = clock64();
 
     // ========================================== linear step (whole warp)
-    const StepOut<T> r = linear_step<T, P>(S, Wsrc, dst, newton, tstep, tgoal, lp, fpm_hi_of<P>(a, task),
-                                        gamma_hi_of<P>(a, task), g, hires);
+    const StepOut<T> r = linear_step<T, P>(S, Wsrc, dst, newton, tstep, tgoal, lp, fpm_hi_of<P>(a, ti),
+                                        gamma_hi_of<P>(a, ti), g, hires);
     __syncwarp();
     long long tc3 = clock64();
     if (lane == 0) {
@@ -598,10 +611,10 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         } else {
           // new random patch and SwitchPatch(u, Yn, Yn) (htpytrack.cu:145-151, :204-210)
           const double R = c.patch_range;
-          const uint64_t stream = (uint64_t)(id + c.path_offset);
+          const uint64_t stream = (uint64_t)(lid + c.path_offset);
           for (int e = g; e < NY; e += TEAM)
-            S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(a.seed, stream, rng_index + 2 * e) - R),
-                           T(2.0 * R * frg_uniform01(a.seed, stream, rng_index + 2 * e + 1) - R));
+            S.u[e] = cx<T>(T(2.0 * R * frg_uniform01(pseed, stream, rng_index + 2 * e) - R),
+                           T(2.0 * R * frg_uniform01(pseed, stream, rng_index + 2 * e + 1) - R));
           rng_index += 46;
           __syncwarp(tmask);
           cp d(P(0));
@@ -679,7 +692,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
         const cp* src = final_from_YN ? S.YN : S.Yc;
         for (int e = 0; e < NY; ++e) Yf[e] = cd(src[e]);
         __syncwarp(tmask);
-        team_finish(a, S, Yf, id, task, code, g, tmask, n_ivp, n_newton, step);
+        team_finish(a, S, Yf, id, ti, code, g, tmask, n_ivp, n_newton, step);
       }
       phase = PH_FETCH;
     }

@@ -111,6 +111,16 @@ typedef struct frg_config {
   int lo_final;          /* mixed, mixed_rounds >= 2: 1 = the last round's FP32 kernel keeps paths
                             whose steps are ill conditioned (no hand-off for conditioning); paths
                             then use FP64 only for one bounded segment per earlier round */
+  int carry_handback;    /* mixed, team kernels, frg_track_rounds: 1 = a path that is well
+                            conditioned again in a round's FP64 launch (handback_good / fp64_segment)
+                            continues in the FP32 launch of the round `depth` rounds later on the
+                            same stream, so no launch is added; the last `depth` rounds finish
+                            their paths in FP64. Per path the same computation as frg_track with
+                            mixed_rounds = the rounds left on the path's stream; 0 = a handed-off
+                            path stays in FP64 */
+  int round_graph;       /* frg_track_rounds with carry_handback: 1 = every round's launches, on
+                            every stream, are captured into one CUDA graph and launched once (the
+                            same results); 0 = launched one by one */
 } frg_config;
 
 /* Per-call counters (all paths of the call). */

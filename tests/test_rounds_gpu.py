@@ -69,3 +69,60 @@ def test_rounds_per_round_task_sets():
     assert np.array_equal(codes, np.concatenate([r.codes for r in single]))
     assert np.array_equal(roots, np.concatenate([r.roots for r in single]))
     assert np.array_equal(resid, np.concatenate([r.resid for r in single]))
+
+
+def test_carry_handback_matches_single_calls():
+    """carry_handback: a path handed back by round r's FP64 launch continues in round
+    r + depth's FP32 launch. Per path this is frg_track with mixed_rounds = the number of
+    rounds left on the path's stream (r, r + depth, ...), so the results are equal bit for
+    bit. Short FP64 segments force many hand-backs."""
+    frg_build.build()
+    nrounds, depth = 5, 2
+    sets = np.stack([np.stack([precision_point_task(40 + 2 * r + k, "disk" if k % 2 == 0 else "curve")
+                               for k in range(2)]) for r in range(nrounds)])
+    ppt, seeds = [512, 512], [61, 62, 63, 64, 65]
+    n = sum(ppt)
+    kw = dict(handback_good=4, fp64_segment=16, cond_switch=1e4)
+    cfg = frg.chosen_config(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=1e-8,
+                            carry_handback=1, **kw)
+    with frg.Tracker(cfg) as t:
+        roots = np.zeros((nrounds * n, 21), np.complex128)
+        codes = np.zeros(nrounds * n, np.int32)
+        resid = np.zeros(nrounds * n, np.float64)
+        st = t.track_rounds(sets, ppt, seeds, roots, codes, resid=resid, depth=depth, per_round_tasks=True)
+    assert st["handbacks"] > 0
+    for r in range(nrounds):
+        m = (nrounds - 1 - r) // depth + 1
+        single_cfg = frg.chosen_config(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=1e-8,
+                                       mixed_rounds=m, **kw)
+        with frg.Tracker(single_cfg) as t:
+            want = t.track(sets[r], ppt, seeds[r], want_resid=True)
+        sl = slice(r * n, (r + 1) * n)
+        assert np.array_equal(codes[sl], want.codes), r
+        assert np.array_equal(roots[sl], want.roots), r
+        assert np.array_equal(resid[sl], want.resid), r
+
+
+def test_round_graph_matches_stream_launches():
+    """round_graph: the carried rounds captured into one CUDA graph give the results of
+    the same rounds launched one by one, bit for bit, with the same counters."""
+    frg_build.build()
+    nrounds, depth = 6, 3
+    sets = np.stack([np.stack([precision_point_task(70 + r, "disk")]) for r in range(nrounds)])
+    ppt, seeds = [768], [81, 82, 83, 84, 85, 86]
+    out = {}
+    for graph in (0, 1):
+        cfg = frg.chosen_config(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=1e-8,
+                                carry_handback=1, round_graph=graph, handback_good=8, fp64_segment=32)
+        with frg.Tracker(cfg) as t:
+            roots = np.zeros((nrounds * 768, 21), np.complex128)
+            codes = np.zeros(nrounds * 768, np.int32)
+            resid = np.zeros(nrounds * 768, np.float64)
+            st = t.track_rounds(sets, ppt, seeds, roots, codes, resid=resid, depth=depth, per_round_tasks=True)
+        out[graph] = (roots, codes, resid, st)
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][2], out[1][2])
+    for key in ("codes", "ivp_solves", "newton_iters", "fp64_solves", "handbacks"):
+        assert out[0][3][key] == out[1][3][key], key
+    assert out[1][3]["handbacks"] > 0 and out[1][3]["track_ms"] > 0
