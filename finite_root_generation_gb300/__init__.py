@@ -96,7 +96,8 @@ EXPORTS = [
     "frg_track_async", "frg_coll_create", "frg_coll_destroy", "frg_coll_size", "frg_coll_get", "frg_coll_merge",
     "frg_coll_save", "frg_coll_load", "frg_codes_append", "frg_lambertw0", "frg_estimate_collected",
     "frg_track_noalloc", "frg_track_rounds", "frg_set_mlp", "frg_track_features", "frg_mlp_param_count",
-    "frg_mlp_grad", "frg_mlp_train", "frg_mlp_predict",
+    "frg_mlp_grad", "frg_mlp_train", "frg_mlp_predict", "frg_dcoll_create", "frg_dcoll_destroy", "frg_dcoll_merge",
+    "frg_dcoll_size", "frg_dcoll_get",
 ]
 NOALLOC_MAX_TASKS = 1024
 
@@ -151,6 +152,12 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_coll_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.frg_coll_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.frg_codes_append.argtypes = [ctypes.c_char_p, _I32, ctypes.c_int64]
+    lib.frg_dcoll_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int64, ctypes.c_double]
+    lib.frg_dcoll_destroy.argtypes = [ctypes.c_void_p]
+    lib.frg_dcoll_merge.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p]
+    lib.frg_dcoll_size.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+    lib.frg_dcoll_get.argtypes = [ctypes.c_void_p, _D, _I32, ctypes.c_int64]
     lib.frg_track_noalloc.argtypes = [ctypes.POINTER(FrgConfig), ctypes.c_void_p, ctypes.c_int, _I64,
                                       ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
@@ -368,6 +375,59 @@ class Collection:
     def load(self, path: str):
         if self.lib.frg_coll_load(self._c, path.encode()) != 0:
             raise FrgError(f"cannot read {path} (missing, truncated or unsorted)")
+
+
+class DeviceCollection:
+    """Device-resident root collection (``frg_dcoll``): duplicate marking on the GPU with
+    the host Collection's rule, one collection per key (e.g. per task)."""
+
+    def __init__(self, capacity: int, dup_tol: float = 1e-6, device: int = 0):
+        self.lib = load()
+        self._c = ctypes.c_void_p()
+        st = self.lib.frg_dcoll_create(ctypes.byref(self._c), int(device), ctypes.c_int64(capacity),
+                                       ctypes.c_double(dup_tol))
+        if st != 0:
+            raise FrgError(f"frg_dcoll_create failed ({st})")
+
+    def close(self):
+        if self._c:
+            self.lib.frg_dcoll_destroy(self._c)
+            self._c = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def merge(self, roots, codes, keys=None, stream=0):
+        """Merge device buffers (torch CUDA tensors): roots [n, 42] float64, codes [n]
+        int32 (marked 6 in place), keys [n] int32 or None."""
+        n = int(codes.numel())
+        st = self.lib.frg_dcoll_merge(self._c, _ptr(roots), _ptr(codes), _ptr(keys), ctypes.c_int64(n),
+                                      ctypes.c_void_p(stream))
+        if st != 0:
+            raise FrgError(f"frg_dcoll_merge failed ({st})")
+
+    def size(self, stream=0) -> int:
+        n = ctypes.c_int64()
+        st = self.lib.frg_dcoll_size(self._c, ctypes.c_void_p(stream), ctypes.byref(n))
+        if st != 0:
+            raise FrgError(f"frg_dcoll_size failed ({st})")
+        return int(n.value)
+
+    def __len__(self) -> int:
+        return self.size()
+
+    def roots(self):
+        """(roots [m, 21] complex, keys [m]) in collection order."""
+        m = self.size()
+        out = np.zeros((m, NV), np.complex128)
+        keys = np.zeros(m, np.int32)
+        if m and self.lib.frg_dcoll_get(self._c, out.ctypes.data_as(_D), keys.ctypes.data_as(_I32),
+                                        ctypes.c_int64(m)) != 0:
+            raise FrgError("frg_dcoll_get failed")
+        return out, keys
 
 
 def codes_append(path: str, codes) -> None:

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfrg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["frg_track.cu", "frg_track_team.cu", "frg_capi.cu", "frg_noalloc.cu", "frg_mlp.cu"]
+CUDA_SOURCES = ["frg_track.cu", "frg_track_team.cu", "frg_capi.cu", "frg_noalloc.cu", "frg_mlp.cu", "frg_dcoll.cu"]
 # The tracking kernels' FP32 arithmetic is checked by residuals and finished in FP64,
 # so FP32 division and square root use the fast approximate forms (a few ulp) and FP32
 # subnormals flush to zero; FP64 arithmetic is unaffected by these flags.

@@ -270,6 +270,31 @@ frg_status frg_coll_save(const frg_coll* coll, const char* fpt_coll_path);
 frg_status frg_coll_load(frg_coll* coll, const char* fpt_coll_path);
 frg_status frg_codes_append(const char* error_codes_path, const int32_t* codes, int64_t n);
 
+/* ---- device-resident root collection: SortingDeletingMerging (frgsupport.cu:10-215)
+ *      and the thrust ordering of frg.cu:432-435 on the GPU, across rounds, one
+ *      collection per key (e.g. per task) ---- */
+typedef struct frg_dcoll frg_dcoll;
+
+/* A collection of at most `capacity` roots on `device` (device memory: 336 bytes per root
+ * plus a hash table of 16 bytes per slot, 2 to 4 slots per root); dup_tol > 0. */
+frg_status frg_dcoll_create(frg_dcoll** coll, int device, int64_t capacity, double dup_tol);
+void frg_dcoll_destroy(frg_dcoll* coll);
+/* Merge n roots (device memory: roots n x 21 complex, codes n int32, keys n int32 in
+ * [0, 2^20) or NULL for key 0) on `stream`: the same marks as frg_coll_merge applied per
+ * key -- a success (code 0) within dup_tol in every real component of a collected root
+ * of its key, or of a lower-index success of the same call and key that is itself not a
+ * duplicate, becomes code 6 in place; the others are collected. A root whose first
+ * component is not finite matches nothing. Asynchronous; merges on one collection must
+ * be ordered (one stream, or events). */
+frg_status frg_dcoll_merge(frg_dcoll* coll, const double* roots, int32_t* codes, const int32_t* keys, int64_t n,
+                           void* stream);
+/* Roots collected so far (synchronizes `stream`); FRG_ERR_ALLOC if a merge ran out of
+ * capacity (the roots past it were marked kept but not collected). */
+frg_status frg_dcoll_size(frg_dcoll* coll, void* stream, int64_t* size);
+/* Copy the collected roots (in collection order, not sorted) and their keys (optional)
+ * to host memory; synchronizes the device. */
+frg_status frg_dcoll_get(frg_dcoll* coll, double* roots, int32_t* keys, int64_t capacity);
+
 /* ---- statistics (frgsupport.cu:220-272, frg.cu:463-464) ---- */
 /* Principal branch of the Lambert W function. */
 double frg_lambertw0(double z);
