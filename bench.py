@@ -306,25 +306,39 @@ class TaskCollections:
         return c.roots() if c is not None else np.zeros((0, 21), np.complex128)
 
 
-def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world):
+def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world, dedup=None):
     """K rounds through frg_track_rounds (device buffers, `depth` rounds in flight, one
-    task set per round), bracketed by a barrier and a synchronize on both sides. The
-    library times the span with CUDA events on its launching streams (first launch to
-    the last round's end); torch events on the current stream bracket the call as a
-    cross-check."""
+    task set per round), then, with dedup = (DeviceCollection, keys), the duplicate
+    removal of every round's roots on the device; bracketed by a barrier and a
+    synchronize on both sides. Returns (stats, ms): the library times the tracking span
+    with CUDA events on its launching streams (first launch to the last round's end) and
+    the merges are timed with CUDA events on the stream they run on (torch's current
+    stream); ms = tracking span + merges."""
     roots, codes, resid = outs
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record()
     st = tracker.track_rounds(fpm_sets, ppt, seeds, roots, codes, resid=resid, depth=depth, per_round_tasks=True)
-    ev1.record()
+    merge_ms = 0.0
+    if dedup is not None:
+        dc, keys = dedup
+        n = keys.numel()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.current_stream().cuda_stream
+        ev0.record()
+        for i in range(len(seeds)):
+            sl = slice(i * n, (i + 1) * n)
+            good = (codes[sl] == 0) & (resid[sl] <= RESID_MAX)
+            mc = torch.where(good, 0, 5).to(torch.int32)
+            dc.merge(roots[sl], mc, keys[i], stream=stream)
+        ev1.record()
+        torch.cuda.synchronize()
+        merge_ms = ev0.elapsed_time(ev1)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    return st, ev0.elapsed_time(ev1)
+    return st, st["track_ms"] + merge_ms, merge_ms
 
 
 def _collect(frg, wl, steps, outs, n):
@@ -381,14 +395,29 @@ def run_ours(args, rank, world):
                            resid=outs[2], depth=1, per_round_tasks=True)
     torch.cuda.synchronize()
 
-    # ---- chosen configuration, task sets resident in HBM (value) ----
+    # device duplicate removal: one collection per global task (key), keys of each step
+    keys = [torch.from_numpy(np.repeat(np.asarray(wl.step_tasks(s), np.int32), wl.paths_per_task)).cuda()
+            for s in steps]
+    capacity = k * n + 1024
+
+    # ---- chosen configuration, task sets resident in HBM (value): tracking and the
+    #      device duplicate removal of every round ----
     c_outs = tuple(o[: k * n] for o in outs)
+    c_dc = frg.DeviceCollection(capacity, DUP_TOL, device=dev)
     with ClockSampler(dev) as clk:
-        c_st, c_torch_ms = _timed_rounds(torch, chosen, d_sets, ppt, seeds, c_outs, depth, world)
+        c_st, c_ms, c_merge_ms = _timed_rounds(torch, chosen, d_sets, ppt, seeds, c_outs, depth, world,
+                                               dedup=(c_dc, keys))
     clocks = clk.summary()
+    c_dev_distinct = len(c_dc)
+    c_dc.close()
     c_coll = _collect(frg, wl, steps, c_outs, n)
+    if c_dev_distinct != c_coll.distinct():
+        raise SystemExit(f"device and host duplicate removal disagree: {c_dev_distinct} vs {c_coll.distinct()}")
     # ---- plain FP64 on the same steps, seeds and pipelining (ratio and recall) ----
-    p_st, _ = _timed_rounds(torch, plain, d_sets, ppt, seeds, c_outs, depth, world)
+    p_dc = frg.DeviceCollection(capacity, DUP_TOL, device=dev)
+    p_st, p_ms, _ = _timed_rounds(torch, plain, d_sets, ppt, seeds, c_outs, depth, world, dedup=(p_dc, keys))
+    p_dev_distinct = len(p_dc)
+    p_dc.close()
     p_coll = _collect(frg, wl, steps, c_outs, n)
     hits = found = 0
     for t in sorted(p_coll.colls):
@@ -398,7 +427,7 @@ def run_ours(args, rank, world):
     rec = hits / max(found, 1)
     # ---- one round of the chosen configuration with nothing else in flight: its FP32 and
     #      FP64 stages' own durations (the pipelined rounds overlap them) ----
-    solo_st, _ = _timed_rounds(torch, chosen, d_sets[:1], ppt, seeds[:1], tuple(o[:n] for o in outs), 1, world)
+    solo_st, _, _ = _timed_rounds(torch, chosen, d_sets[:1], ppt, seeds[:1], tuple(o[:n] for o in outs), 1, world)
 
     # ---- end to end through the C ABI with pinned host buffers (e2e): the task upload,
     #      tracking, the copy of roots/codes/residuals back, and the host duplicate merge
@@ -421,10 +450,9 @@ def run_ours(args, rank, world):
     e2e_distinct = e2e_coll.distinct()
     e2e_s = time.perf_counter() - t0
 
-    track_ms = c_st["track_ms"]
-    p_ms = p_st["track_ms"]
-    distinct = c_coll.distinct()
-    p_distinct = p_coll.distinct()
+    track_ms = c_ms
+    distinct = c_dev_distinct
+    p_distinct = p_dev_distinct
     t = torch.tensor([track_ms, e2e_s, distinct, e2e_distinct, p_ms, p_distinct, hits, found],
                      dtype=torch.float64)
     if world > 1:
@@ -435,6 +463,7 @@ def run_ours(args, rank, world):
         distinct, e2e_distinct, p_distinct = float(tsum[2]), float(tsum[3]), float(tsum[5])
         rec = float(tsum[6]) / max(float(tsum[7]), 1.0)
     chosen_rounds = chosen.config.mixed_rounds
+    chosen_carry = bool(chosen.config.carry_handback) and chosen_rounds <= 1
     chosen.close()
     plain.close()
     if rank != 0:
@@ -496,7 +525,7 @@ def run_ours(args, rank, world):
         "speedup_vs_plain_fp64": round(value / value_plain, 3),
         "recall_vs_plain_fp64": round(rec, 5),
         "distinct_roots": int(distinct),
-        "torch_event_ms": round(c_torch_ms, 1),
+        "dedup_ms_per_step": round(c_merge_ms / k, 3),
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fma (fp32 + fp64 pipes)", "achieved": round(frac, 5), "peak": 1.0,
                      "unit": "fraction of the step's time the algorithmic FLOPs need at the measured FP32 and "
@@ -510,9 +539,10 @@ def run_ours(args, rank, world):
                      "kernels_one_round_alone": {
                          kk: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
                          for kk, v in kernels.items()}},
-        # per round: start values, FP32 and double-float parameter copies, then per mixed
-        # round one FP32-stage and one FP64-stage tracking kernel
-        "gpu_launches": (3 + 2 * max(1, chosen_rounds)) * k,
+        # tracking: with carry hand-back the FP32 and double-float parameter copies once,
+        # then per round the start values, the FP32-stage and the FP64-stage kernels;
+        # without it all five per round (two per mixed round); dedup: five kernels per round
+        "gpu_launches": ((2 + 3 * k) if chosen_carry else (3 + 2 * max(1, chosen_rounds)) * k) + 5 * k,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
