@@ -357,6 +357,41 @@ class RefLib:
         return self.lib.ref_lambertw(float(z))
 
 
+def cognate34_linkage(x, P0):
+    """The 3/4 cognate of one half of a Stephenson II linkage (A, B, C, D, F, G, H; seven
+    complex values) with precision point P0: two similarity maps that keep B and F
+    (frgkinematics.cu:140-182, Dijksman's construction; dead code in the reference, its
+    calls commented out at :262-266)."""
+    A, B, C, D, F, G, H = x
+    s = (H - G) / (C - G)
+    Ap, Bp, Cp, Gp = s * (A - D) + D, s * (B - D) + D, s * (C - D) + D, D + (H - G)
+    s2 = (B - F) / (Bp - F)
+    return np.array([s2 * (Ap - F) + F, B, s2 * (Cp - F) + F, s2 * (D - F) + F, F, s2 * (Gp - F) + F,
+                     s2 * (H - F) + F])
+
+
+def cognate12_root(z, q):
+    """The 1/2 cognate of a dehomogenized root z (21 complex) of task q: Cognate12 on both
+    halves and the rotations U_down (frgkinematics.cu:185-256)."""
+    z = np.asarray(z, np.complex128)
+    B, F = z[1], z[4]
+    P, Pc = q[0:8], q[8:16]
+    out = z.copy()
+    out[14:21] = ((P[1:8] - B) - z[14:21] * (P[0] - F)) / (F - B)
+
+    def c12(x, p0):
+        A, B, C, D, F, G, H = x
+        s = (B - F) / (D - F)
+        Dp, Gp = s * (D - H) + H, s * (G - H) + H
+        s2 = (p0 - F) / (H - F)
+        return np.array([s2 * (A - B) + B, B, s2 * (C - B) + B, s2 * (Dp - B) + B, B + (p0 - F), s2 * (Gp - B) + B,
+                         s2 * (H - B) + B])
+
+    out[0:7] = c12(z[0:7], P[0])
+    out[7:14] = c12(z[7:14], Pc[0])
+    return out
+
+
 # The reference's hard-coded target (frg.cu:149-178) and gamma (frg.cu:41).
 T_REF = np.array([
     4.241713408139979 - 4.925334736425448j, 1.448005491494222 - 2.686249989236069j,
