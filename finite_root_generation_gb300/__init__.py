@@ -76,7 +76,7 @@ class FrgStats(ctypes.Structure):
         ("kernel_cycles", ctypes.c_int64 * 12), ("handbacks", ctypes.c_int64),
         ("refine_solves", ctypes.c_int64), ("refine_warp_steps", ctypes.c_int64),
         ("round_ms", ctypes.c_double * 32), ("fp64_segment_hist", ctypes.c_int64 * 6),
-        ("fp64_segment_max", ctypes.c_int64), ("retired", ctypes.c_int64),
+        ("fp64_segment_max", ctypes.c_int64), ("retired", ctypes.c_int64), ("refine_cycles", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -87,7 +87,8 @@ class FrgStats(ctypes.Structure):
                 "kernel_cycles": list(self.kernel_cycles), "handbacks": self.handbacks,
                 "refine_solves": self.refine_solves, "refine_warp_steps": self.refine_warp_steps,
                 "round_ms": list(self.round_ms), "fp64_segment_hist": list(self.fp64_segment_hist),
-                "fp64_segment_max": self.fp64_segment_max, "retired": self.retired}
+                "fp64_segment_max": self.fp64_segment_max, "retired": self.retired,
+                "refine_cycles": self.refine_cycles}
 
 
 # Exported symbols of libfrg_gb300.so, one per declaration in include/frg_gb300.h.

@@ -168,7 +168,7 @@ frg_status frg_check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->mixed_rounds < 0 || c->mixed_rounds > 64) return fail(ctx, FRG_ERR_ARG, "mixed_rounds must be in 0..64");
   if (c->path_offset < 0) return fail(ctx, FRG_ERR_ARG, "path_offset must be non-negative");
   if (c->fp64_budget < 0) return fail(ctx, FRG_ERR_ARG, "fp64_budget must be non-negative");
-  if (c->lo_refine < 0 || c->lo_refine > 2) return fail(ctx, FRG_ERR_ARG, "lo_refine must be 0, 1 or 2");
+  if (c->lo_refine < 0 || c->lo_refine > 3) return fail(ctx, FRG_ERR_ARG, "lo_refine must be 0, 1, 2 or 3");
   if (c->lo_points < 0 || c->lo_points > 1) return fail(ctx, FRG_ERR_ARG, "lo_points must be 0 or 1");
   if (c->lo_final < 0 || c->lo_final > 1) return fail(ctx, FRG_ERR_ARG, "lo_final must be 0 or 1");
   if (c->carry_handback < 0 || c->carry_handback > 1) return fail(ctx, FRG_ERR_ARG, "carry_handback must be 0 or 1");
@@ -462,6 +462,7 @@ static void add_counters(frg_stats* st, const unsigned long long* cnt, bool mixe
     if ((int64_t)cnt[46] > st->fp64_segment_max) st->fp64_segment_max = (int64_t)cnt[46];
     st->refine_solves += (int64_t)cnt[22];
     st->refine_warp_steps += (int64_t)cnt[23];
+    st->refine_cycles += (int64_t)cnt[37];
   }
 }
 

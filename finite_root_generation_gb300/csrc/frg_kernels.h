@@ -32,7 +32,8 @@ struct Handoff {
 constexpr int FRG_START_STRIDE = 51;
 // counters: codes[8], ivp, newton, steps, fp64 solves, handoffs, hand-backs, -, -, handoff
 // reasons 1..6 at [16..21], refinement solves and warp steps at [22..23], kernel cycles at
-// [24..35], -, FP64-segment histogram at [40..45], longest FP64 segment at [46]
+// [24..35], retired paths at [36], FP32-stage refinement-residual cycles at [37],
+// FP64-segment histogram at [40..45], longest FP64 segment at [46]
 #define FRG_NCOUNTERS 48
 
 struct TrackArgs {

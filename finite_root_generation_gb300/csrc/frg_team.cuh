@@ -124,6 +124,7 @@ struct StepOut {
   T ratio;   // condition estimate (pivot ratios of the elimination), +inf if not finite
   T xnorm2;  // |x|^2 of the (normalised, for tangents) solution
   T hnorm;   // |H| at the evaluation point (Newton)
+  long long res_cycles;  // cycles the warp spent in the refinement residual (FP32 stage)
 };
 
 // The team's residual F_j (its three equations) at the point Yd with q(t), all in
@@ -222,6 +223,8 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T, P>& S, const cx<T>* Ws
   // ---- FP64 residual of the corrector (FP32 stage only)
   cx<T> hF0 = zero, hF1 = zero, hF2 = zero, hU = zero;
   T hsq = T(0);
+  long long res_cycles = 0;
+  const long long t_res0 = LOWP ? clock64() : 0;
   if (LOWP && newton && hires) {
     cx<P> fI, fII, fIII;
     residual_hi<P>(S.YN, S.spm, fpm_hi, gamma_hi, j, fI, fII, fIII);
@@ -232,6 +235,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T, P>& S, const cx<T>* Ws
     hF0 = cx<T>(fI); hF1 = cx<T>(fII); hF2 = cx<T>(fIII); hU = cx<T>(d);
     hsq = grp ? T(cnorm2(hF0) + cnorm2(hF1) + cnorm2(hF2)) : T(cnorm2(hU));
   }
+  if (LOWP) res_cycles = clock64() - t_res0;
 
   // ---- evaluation point and parameters q(t), dq/dt (htpysupport.cu:37-62)
   const cx<T> A = S.Ye[0], B = S.Ye[1], C = S.Ye[2], D = S.Ye[3], F = S.Ye[4], G = S.Ye[5], H = S.Ye[6];
@@ -418,6 +422,7 @@ __device__ __forceinline__ StepOut<T> linear_step(Smem<T, P>& S, const cx<T>* Ws
   for (int c = 0; c < 16; ++c) n2 += cnorm2(xg[c]);
   n2 += team_sum(FULL, grp ? cnorm2(xu) : T(0));
   StepOut<T> out;
+  out.res_cycles = res_cycles;
   out.hnorm = sqrt(team_sum(FULL, hsq));
   out.ratio = (n2 - n2 == T(0)) ? ratio : T(INFINITY);  // n2 - n2 is NaN iff n2 is not finite
   if (!newton) {

@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
   // cycle accounting (lane 0 of each warp): fetch, setup, linear step, transitions;
   // warp steps and active-team steps
   long long cyc[4] = {0, 0, 0, 0};
-  long long warp_steps = 0, team_steps = 0, refine_steps = 0, refine_warp = 0;
+  long long warp_steps = 0, team_steps = 0, refine_steps = 0, refine_warp = 0, res_cyc = 0;
   __syncwarp();
 
   for (;;) {
@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     if (lane == 0) {
       cyc[0] += tc1 - tc0; cyc[1] += tc2 - tc1; cyc[2] += tc3 - tc2;
       warp_steps++;
+      res_cyc += r.res_cycles;
     }
     {
       const unsigned act = __ballot_sync(FULL, phase != PH_IDLE && g == 0);
@@ -545,9 +546,16 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
           if (LO && !hires) {
             // FP32 residuals: at the FP32 noise floor either accept (no refinement) or
             // continue on double-float residuals to the reference's tolerance
-            const bool floor_ = residual < T(c.newt_tol_lo) || (it > 1 && residual > T(0.5) * res_prev);
-            if (floor_ && c.lo_refine) hires = true;
-            if ((floor_ && !c.lo_refine) || !(it < max_its)) done = true;
+            const bool conv = residual < T(c.newt_tol_lo);
+            const bool floor_ = conv || (it > 1 && residual > T(0.5) * res_prev);
+            if (c.lo_refine == 3 && conv && !sharp) {
+              // the FP32 update is already below newt_tol_lo: accept it without refining
+              done = true;
+              predicted = true;
+            } else {
+              if (floor_ && c.lo_refine) hires = true;
+              if ((floor_ && !c.lo_refine) || !(it < max_its)) done = true;
+            }
           } else if (!(it < max_its && residual > tol)) {
             done = true;
           } else if (LO && !sharp && c.lo_refine == 2 &&
@@ -706,6 +714,7 @@ __global__ void __launch_bounds__(FRG_TEAM_THREADS) team_kernel(TrackArgs a) {
     if (LO) {
       atomicAdd(&a.counters[22], (unsigned long long)refine_steps);
       atomicAdd(&a.counters[23], (unsigned long long)refine_warp);
+      atomicAdd(&a.counters[37], (unsigned long long)res_cyc);
     }
   }
 }

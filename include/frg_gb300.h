@@ -94,8 +94,10 @@ typedef struct frg_config {
                             FP64 returns to FP32 in the next round (1 = no return) */
   int lo_refine;         /* mixed: 1 = the FP32 corrector refines on residuals in the point type
                             (lo_points) to newt_tol; 2 = the same, but a refined iteration whose
-                            successor is predicted below newt_tol / 10 ends it; 0 = it stops at
-                            newt_tol_lo */
+                            successor is predicted below newt_tol / 10 ends it; 3 = a corrector
+                            whose FP32 update falls below newt_tol_lo is accepted without
+                            refinement, one that stalls above it refines as in 1; 0 = it stops
+                            at newt_tol_lo */
   int lo_endgame;        /* mixed: 1 = the FP32 stage (with refinement) also runs the endgame and
                             sharpening, FP64 only for ill-conditioned steps; 0 = FP64 from t_switch */
   int64_t path_offset;   /* random stream of local path i is path_offset + i: shards of one round
@@ -149,6 +151,8 @@ typedef struct frg_stats {
                                    <10000, >=10000 FP64 solves in it */
   int64_t fp64_segment_max;     /* mixed: most FP64 solves one path spent in one FP64 launch */
   int64_t retired;              /* paths the early-retirement network ended (reported as code 2) */
+  int64_t refine_cycles;        /* mixed: FP32-stage cycles (summed over warps) spent evaluating the
+                                   double-float refinement residuals, part of kernel_cycles[2] */
 } frg_stats;
 
 typedef struct frg_ctx frg_ctx;
