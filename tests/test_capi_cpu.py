@@ -133,7 +133,7 @@ def test_invalid_configs_rejected_before_any_cuda_call():
     import ctypes
 
     lib = frg.load()
-    bad = [dict(lo_refine=3), dict(lo_points=2), dict(fp64_budget=-1), dict(mixed_rounds=65), dict(path_offset=-1),
+    bad = [dict(lo_refine=4), dict(lo_points=2), dict(fp64_budget=-1), dict(mixed_rounds=65), dict(path_offset=-1),
            dict(lo_final=2), dict(fp64_segment=-5), dict(handback_good=-1), dict(precision=7),
            dict(kernel_variant=9), dict(rk_tol=0.0), dict(newt_attempts=0),
            dict(precision=frg.PREC_MIXED, cond_switch=0.5)]
