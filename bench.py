@@ -270,11 +270,13 @@ def flops_per_solve():
 
 # ---------------------------------------------------------------------- our impl
 def _chosen_overrides(frg):
-    """The chosen configuration on top of the workload's (frg.CHOSEN): mixed precision, the
-    FP32 stage also running the endgame and sharpening (double-float refinement), FP64 for
-    steps whose condition estimate exceeds 1e5 and for finishing every root, and at most
-    10,000 FP64 solves per path (a path still going after that ends as a step-limit
-    failure; such paths are crawling near a singularity and set the FP64 tail)."""
+    """The chosen configuration on top of the workload's (frg.CHOSEN): mixed precision,
+    the FP32 stage also running the endgame and sharpening (double-float points and
+    refinement), FP64 for steps whose condition estimate exceeds 5e5 and for finishing
+    every root, at most 10,000 FP64 solves per path and launch (a path still going after
+    that ends as a step-limit failure; such paths crawl near a singularity and set the
+    FP64 tail), paths well conditioned again carried back to FP32 in a later round, the
+    rounds launched as one CUDA graph."""
     return dict(frg.CHOSEN)
 
 
@@ -513,8 +515,10 @@ def run_ours(args, rank, world):
                    "paths_per_step": n, "tasks_per_step": wl.tasks_per_step, "steps_cover_workload": k >= wl.blocks,
                    "rounds_in_flight": depth,
                    "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
-                             "sharpening included), FP64 team kernel for steps with condition estimate > 1e5 "
-                             "(at most 10,000 FP64 solves per path) and for finishing",
+                             "sharpening included), FP64 team kernel for steps with condition estimate > 5e5 "
+                             "(at most 10,000 FP64 solves per path and launch) and for finishing; paths well "
+                             "conditioned again carried back to FP32 in a later round; rounds as one CUDA graph; "
+                             "duplicate removal on the device",
                    "l2": f"not flushed: per-round state (start values 816 B, hand-off record 1.2 KB, outputs "
                          f"348 B per path: ~{n * 2364 / 1e6:.0f} MB per round, {depth} rounds in flight) exceeds "
                          "the 129 MB L2",
@@ -638,6 +642,29 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_profile_case(args):
+    """The ncu target: one round of the chosen configuration (or plain FP64 with
+    --profile-plain) on --profile-paths paths of the workload's first two tasks, one
+    call, nothing else launched. Prints the call's counters."""
+    import finite_root_generation_gb300 as frg
+    from finite_root_generation_gb300 import build as frg_build
+
+    frg_build.build()
+    wl = Workload(args.workload)
+    tasks = wl.tasks[:2] if wl.ntasks >= 2 else wl.tasks
+    ppt = [args.profile_paths // len(tasks)] * len(tasks)
+    cfg = workload_config(frg, frg.PREC_FP64 if args.profile_plain else frg.PREC_MIXED)
+    if not args.profile_plain:
+        for key, v in _chosen_overrides(frg).items():
+            setattr(cfg, key, v)
+    with frg.Tracker(cfg) as t:
+        r = t.track(tasks, ppt, SEED_BASE, want_resid=True)
+    keys = ("ivp_solves", "newton_iters", "fp64_solves", "refine_solves", "refine_warp_steps", "refine_cycles",
+            "track_ms", "stage_ms", "kernel_cycles", "codes")
+    print(json.dumps({"profile_case": {"paths": sum(ppt), "plain": bool(args.profile_plain)},
+                      **{k: r.stats[k] for k in keys}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -648,7 +675,14 @@ def main():
     ap.add_argument("--depth", type=int, default=4, help="rounds in flight")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one chosen-configuration round on --profile-paths paths (an ncu target), nothing else")
+    ap.add_argument("--profile-paths", type=int, default=4096)
+    ap.add_argument("--profile-plain", action="store_true", help="with --profile-case: plain FP64 instead")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("need --steps >= 1 and --warmup >= 0")
     world = int(os.environ.get("WORLD_SIZE", "1"))
