@@ -324,7 +324,7 @@ def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world, dedu
     merge_ms = 0.0
     if dedup is not None:
         dc, keys = dedup
-        n = keys.numel()
+        n = keys[0].numel()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         stream = torch.cuda.current_stream().cuda_stream
@@ -371,6 +371,13 @@ def run_ours(args, rank, world):
     chosen_cfg = workload_config(frg, frg.PREC_MIXED)
     for key, v in _chosen_overrides(frg).items():
         setattr(chosen_cfg, key, v)
+    # the autotuner's recorded choice for this GPU and workload, where there is one
+    from finite_root_generation_gb300 import autotune
+    tuned = autotune.tuned_setting(torch.cuda.get_device_name(dev), args.workload)
+    if tuned:
+        depth = int(tuned.pop("depth", depth))
+        for key, v in tuned.items():
+            setattr(chosen_cfg, key, v)
     chosen = frg.Tracker(chosen_cfg, device=dev)
     plain = frg.Tracker(workload_config(frg, frg.PREC_FP64), device=dev)
     # steps of this rank (ranks take disjoint seeds)
@@ -514,6 +521,8 @@ def run_ours(args, rank, world):
                                "checks, one duplicate collection per task over the timed steps",
                    "paths_per_step": n, "tasks_per_step": wl.tasks_per_step, "steps_cover_workload": k >= wl.blocks,
                    "rounds_in_flight": depth,
+                   "setting_from": "autotuner table (finite_root_generation_gb300/tuned.json)" if tuned
+                                   else "frg.CHOSEN",
                    "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
                              "sharpening included), FP64 team kernel for steps with condition estimate > 5e5 "
                              "(at most 10,000 FP64 solves per path and launch) and for finishing; paths well "
