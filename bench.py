@@ -579,8 +579,11 @@ def cpu_baseline(args, wl, steps, paths_per_task, seed_base=SEED_BASE):
     step, the first `paths_per_task` paths of each of its tasks, with the step's seed,
     path streams and gammas. Uses the reference's own sources built for the host
     (oracle/_ref/libfrgref.so, kind "reference") where they were staged, else the oracle's
-    C restatement (kind "port"); duplicates are removed with the same library's merge
-    (SortingDeletingMerging, or the restatement's). Never loads the product library."""
+    C restatement (kind "port"). Duplicates are removed with the oracle's restatement of
+    SortingDeletingMerging (pinned to the reference's merge by the golden vectors): the
+    reference's own merge reads one element past its local order vector in its fold loop
+    (frgsupport.cu:195), which crashed the host process once collections grew past a
+    round. Never loads the product library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -588,6 +591,7 @@ def cpu_baseline(args, wl, steps, paths_per_task, seed_base=SEED_BASE):
     cores = os.cpu_count() or 1
     use_ref = os.path.exists(oracle.REF_SO)
     lib = oracle.RefLib() if use_ref else oracle.Oracle()
+    merger = oracle.Oracle()
     o_cfg = None if use_ref else lib.config(start_dist=1)
     colls = {}
     total_paths = 0
@@ -609,12 +613,8 @@ def cpu_baseline(args, wl, steps, paths_per_task, seed_base=SEED_BASE):
             finite = np.abs(yf[:, 21]) >= INF_TOL * zmax
             good = (codes == 0) & finite & (resid <= RESID_MAX)
             c = np.where(good, 0, 5).astype(np.int32)
-            order = np.argsort(roots[:, 0].real, kind="stable").astype(np.int32)
             coll = colls.get(kt, np.zeros((0, 21), np.complex128))
-            if use_ref:
-                colls[kt], _ = lib.sort_merge(coll, roots, c, order)
-            else:
-                colls[kt], _ = lib.sort_merge(coll, roots, c, DUP_TOL)
+            colls[kt], _ = merger.sort_merge(coll, roots, c, DUP_TOL)
             total_paths += paths_per_task
     dt = time.perf_counter() - t0
     d = sum(len(c) for c in colls.values())
@@ -622,8 +622,10 @@ def cpu_baseline(args, wl, steps, paths_per_task, seed_base=SEED_BASE):
             "distinct": d, "paths": total_paths, "seconds": round(dt, 2),
             "sample": f"first {paths_per_task} paths of each task of step(s) {steps[0]}..{steps[-1]} "
                       f"({total_paths} paths, the GPU arm's seeds and path streams), {dt:.1f} s on {cores} threads; "
-                      + ("the reference's own tracker sources built for this host (oracle/_ref/libfrgref.so), "
-                         "duplicates by its SortingDeletingMerging" if use_ref else
+                      + ("the reference's own tracker sources built for this host (oracle/_ref/libfrgref.so); "
+                         "duplicates by the oracle's restatement of SortingDeletingMerging (the reference's own "
+                         "reads past its order vector, frgsupport.cu:195, and crashed on grown collections)"
+                         if use_ref else
                          "the oracle's C restatement (the reference's sources were not staged)")}
 
 

@@ -71,13 +71,12 @@ class RefGPU:
 
 
 def _distinct(roots, codes, resid, dup_tol=1e-6):
-    """Distinct finite roots with the reference's own merge (SortingDeletingMerging)."""
+    """Distinct finite roots with the oracle's restatement of SortingDeletingMerging (the
+    reference's own reads past its order vector, frgsupport.cu:195)."""
     import oracle
-    ref = oracle.RefLib()
     good = (codes == 0) & (resid <= 1e-10)
     c = np.where(good, 0, 5).astype(np.int32)
-    order = np.argsort(roots[:, 0].real, kind="stable").astype(np.int32)
-    coll, _ = ref.sort_merge(np.zeros((0, 21), np.complex128), roots, c, order)
+    coll, _ = oracle.Oracle().sort_merge(np.zeros((0, 21), np.complex128), roots, c, dup_tol)
     return coll
 
 
