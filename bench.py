@@ -323,17 +323,18 @@ def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world, dedu
     st = tracker.track_rounds(fpm_sets, ppt, seeds, roots, codes, resid=resid, depth=depth, per_round_tasks=True)
     merge_ms = 0.0
     if dedup is not None:
-        dc, keys = dedup
+        # the merges mark duplicates in a copy of the codes (made by the copy engine), so the
+        # tracker's own codes stay available for the host cross-check
+        dc, keys, mark = dedup
         n = keys[0].numel()
+        mark.copy_(codes)
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         stream = torch.cuda.current_stream().cuda_stream
         ev0.record()
         for i in range(len(seeds)):
             sl = slice(i * n, (i + 1) * n)
-            good = (codes[sl] == 0) & (resid[sl] <= RESID_MAX)
-            mc = torch.where(good, 0, 5).to(torch.int32)
-            dc.merge(roots[sl], mc, keys[i], stream=stream)
+            dc.merge(roots[sl], mark[sl], keys[i], stream=stream, resid=resid[sl], resid_max=RESID_MAX)
         ev1.record()
         torch.cuda.synchronize()
         merge_ms = ev0.elapsed_time(ev1)
@@ -408,6 +409,7 @@ def run_ours(args, rank, world):
     keys = [torch.from_numpy(np.repeat(np.asarray(wl.step_tasks(s), np.int32), wl.paths_per_task)).cuda()
             for s in steps]
     capacity = k * n + 1024
+    mark = torch.empty(k * n, dtype=torch.int32, device="cuda")
 
     # ---- chosen configuration, task sets resident in HBM (value): tracking and the
     #      device duplicate removal of every round ----
@@ -415,7 +417,7 @@ def run_ours(args, rank, world):
     c_dc = frg.DeviceCollection(capacity, DUP_TOL, device=dev)
     with ClockSampler(dev) as clk:
         c_st, c_ms, c_merge_ms = _timed_rounds(torch, chosen, d_sets, ppt, seeds, c_outs, depth, world,
-                                               dedup=(c_dc, keys))
+                                               dedup=(c_dc, keys, mark))
     clocks = clk.summary()
     c_dev_distinct = len(c_dc)
     c_dc.close()
@@ -424,7 +426,7 @@ def run_ours(args, rank, world):
         raise SystemExit(f"device and host duplicate removal disagree: {c_dev_distinct} vs {c_coll.distinct()}")
     # ---- plain FP64 on the same steps, seeds and pipelining (ratio and recall) ----
     p_dc = frg.DeviceCollection(capacity, DUP_TOL, device=dev)
-    p_st, p_ms, _ = _timed_rounds(torch, plain, d_sets, ppt, seeds, c_outs, depth, world, dedup=(p_dc, keys))
+    p_st, p_ms, _ = _timed_rounds(torch, plain, d_sets, ppt, seeds, c_outs, depth, world, dedup=(p_dc, keys, mark))
     p_dev_distinct = len(p_dc)
     p_dc.close()
     p_coll = _collect(frg, wl, steps, c_outs, n)

@@ -155,8 +155,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_codes_append.argtypes = [ctypes.c_char_p, _I32, ctypes.c_int64]
     lib.frg_dcoll_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int64, ctypes.c_double]
     lib.frg_dcoll_destroy.argtypes = [ctypes.c_void_p]
-    lib.frg_dcoll_merge.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
-                                    ctypes.c_void_p]
+    lib.frg_dcoll_merge.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_double, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
     lib.frg_dcoll_size.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
     lib.frg_dcoll_get.argtypes = [ctypes.c_void_p, _D, _I32, ctypes.c_int64]
     lib.frg_track_noalloc.argtypes = [ctypes.POINTER(FrgConfig), ctypes.c_void_p, ctypes.c_int, _I64,
@@ -405,12 +405,13 @@ class DeviceCollection:
         except Exception:
             pass
 
-    def merge(self, roots, codes, keys=None, stream=0):
+    def merge(self, roots, codes, keys=None, stream=0, resid=None, resid_max=1e-10):
         """Merge device buffers (torch CUDA tensors): roots [n, 42] float64, codes [n]
-        int32 (marked 6 in place), keys [n] int32 or None."""
+        int32 (marked 6 in place), keys [n] int32 or None; with resid [n] float64, a success
+        whose residual exceeds resid_max takes no part."""
         n = int(codes.numel())
-        st = self.lib.frg_dcoll_merge(self._c, _ptr(roots), _ptr(codes), _ptr(keys), ctypes.c_int64(n),
-                                      ctypes.c_void_p(stream))
+        st = self.lib.frg_dcoll_merge(self._c, _ptr(roots), _ptr(codes), _ptr(resid), ctypes.c_double(resid_max),
+                                      _ptr(keys), ctypes.c_int64(n), ctypes.c_void_p(stream))
         if st != 0:
             raise FrgError(f"frg_dcoll_merge failed ({st})")
 

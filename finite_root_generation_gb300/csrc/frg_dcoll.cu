@@ -72,6 +72,12 @@ __device__ __forceinline__ bool cell_of(const double* r, double tol, long long* 
   return true;
 }
 
+// a success that takes part in the merge: code 0 and, when residuals are given, a
+// residual of at most resid_max (a NaN residual fails)
+__device__ __forceinline__ bool takes_part(const int32_t* codes, const double* resid, double resid_max, int64_t t) {
+  return codes[t] == 0 && (!resid || resid[t] <= resid_max);
+}
+
 __device__ __forceinline__ bool same_root(const double* a, const double* b, double tol) {
   for (int k = 0; k < kReals; ++k)
     if (!(fabs(a[k] - b[k]) <= tol)) return false;
@@ -93,9 +99,10 @@ __device__ void table_insert(unsigned long long* tkey, int64_t* tval, unsigned l
 
 // 1. successes matching a collected root of their key become duplicates
 __global__ void __launch_bounds__(kThreads) check_coll(DcollDev c, const double* roots, int32_t* codes,
-                                                      const int32_t* keys, int64_t n, double tol) {
+                                                      const double* resid, double resid_max, const int32_t* keys,
+                                                      int64_t n, double tol) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n || codes[t] != 0) return;
+  if (t >= n || !takes_part(codes, resid, resid_max, t)) return;
   const double* rt = roots + (size_t)t * kReals;
   long long cell;
   if (!cell_of(rt, tol, &cell)) return;
@@ -117,11 +124,11 @@ __global__ void __launch_bounds__(kThreads) check_coll(DcollDev c, const double*
 
 // 2. the remaining successes into the batch table
 __global__ void __launch_bounds__(kThreads) insert_batch(const double* roots, const int32_t* codes,
-                                                        const int32_t* keys, int64_t n, double tol,
-                                                        unsigned long long* bkey, int64_t* bval,
-                                                        unsigned long long bmask) {
+                                                        const double* resid, double resid_max, const int32_t* keys,
+                                                        int64_t n, double tol, unsigned long long* bkey,
+                                                        int64_t* bval, unsigned long long bmask) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n || codes[t] != 0) return;
+  if (t >= n || !takes_part(codes, resid, resid_max, t)) return;
   long long cell;
   if (!cell_of(roots + (size_t)t * kReals, tol, &cell)) return;
   table_insert(bkey, bval, bmask, pack(keys ? keys[t] : 0, cell), t);
@@ -129,13 +136,14 @@ __global__ void __launch_bounds__(kThreads) insert_batch(const double* roots, co
 
 // 3. a success with an earlier matching success of the batch depends on it
 __global__ void __launch_bounds__(kThreads) check_batch(const double* roots, const int32_t* codes,
-                                                       const int32_t* keys, int64_t n, double tol,
-                                                       const unsigned long long* bkey, const int64_t* bval,
-                                                       unsigned long long bmask, unsigned char* dep) {
+                                                       const double* resid, double resid_max, const int32_t* keys,
+                                                       int64_t n, double tol, const unsigned long long* bkey,
+                                                       const int64_t* bval, unsigned long long bmask,
+                                                       unsigned char* dep) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   dep[t] = 0;
-  if (codes[t] != 0) return;
+  if (!takes_part(codes, resid, resid_max, t)) return;
   const double* rt = roots + (size_t)t * kReals;
   long long cell;
   if (!cell_of(rt, tol, &cell)) return;
@@ -216,9 +224,10 @@ __global__ void __launch_bounds__(1024) resolve(const double* roots, int32_t* co
 
 // 5. kept successes join the collection
 __global__ void __launch_bounds__(kThreads) append(DcollDev c, const double* roots, const int32_t* codes,
-                                                  const int32_t* keys, int64_t n, double tol) {
+                                                  const double* resid, double resid_max, const int32_t* keys,
+                                                  int64_t n, double tol) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n || codes[t] != 0) return;
+  if (t >= n || !takes_part(codes, resid, resid_max, t)) return;
   const double* rt = roots + (size_t)t * kReals;
   const unsigned long long slot = atomicAdd(&c.size[0], 1ull);
   if ((int64_t)slot >= c.capacity) {
@@ -307,8 +316,8 @@ extern "C" frg_status frg_dcoll_create(frg_dcoll** out, int device, int64_t capa
   return FRG_OK;
 }
 
-extern "C" frg_status frg_dcoll_merge(frg_dcoll* c, const double* roots, int32_t* codes, const int32_t* keys,
-                                      int64_t n, void* stream) {
+extern "C" frg_status frg_dcoll_merge(frg_dcoll* c, const double* roots, int32_t* codes, const double* resid,
+                                      double resid_max, const int32_t* keys, int64_t n, void* stream) {
   if (!c || n < 0 || (n > 0 && (!roots || !codes))) return FRG_ERR_ARG;
   if (n == 0) return FRG_OK;
   if (cudaSetDevice(c->device) != cudaSuccess) return FRG_ERR_CUDA;
@@ -328,11 +337,12 @@ extern "C" frg_status frg_dcoll_merge(frg_dcoll* c, const double* roots, int32_t
   const unsigned long long bmask = c->bsize - 1;
   if (cudaMemsetAsync(c->bkey, 0xff, sizeof(unsigned long long) * c->bsize, st) != cudaSuccess) return FRG_ERR_CUDA;
   const unsigned grid = (unsigned)((n + kThreads - 1) / kThreads);
-  check_coll<<<grid, kThreads, 0, st>>>(c->d, roots, codes, keys, n, c->tol);
-  insert_batch<<<grid, kThreads, 0, st>>>(roots, codes, keys, n, c->tol, c->bkey, c->bval, bmask);
-  check_batch<<<grid, kThreads, 0, st>>>(roots, codes, keys, n, c->tol, c->bkey, c->bval, bmask, c->dep);
+  check_coll<<<grid, kThreads, 0, st>>>(c->d, roots, codes, resid, resid_max, keys, n, c->tol);
+  insert_batch<<<grid, kThreads, 0, st>>>(roots, codes, resid, resid_max, keys, n, c->tol, c->bkey, c->bval, bmask);
+  check_batch<<<grid, kThreads, 0, st>>>(roots, codes, resid, resid_max, keys, n, c->tol, c->bkey, c->bval, bmask,
+                                         c->dep);
   resolve<<<1, 1024, 0, st>>>(roots, codes, keys, n, c->tol, c->bkey, c->bval, bmask, c->dep);
-  append<<<grid, kThreads, 0, st>>>(c->d, roots, codes, keys, n, c->tol);
+  append<<<grid, kThreads, 0, st>>>(c->d, roots, codes, resid, resid_max, keys, n, c->tol);
   return cudaGetLastError() == cudaSuccess ? FRG_OK : FRG_ERR_CUDA;
 }
 

@@ -287,11 +287,13 @@ void frg_dcoll_destroy(frg_dcoll* coll);
  * [0, 2^20) or NULL for key 0) on `stream`: the same marks as frg_coll_merge applied per
  * key -- a success (code 0) within dup_tol in every real component of a collected root
  * of its key, or of a lower-index success of the same call and key that is itself not a
- * duplicate, becomes code 6 in place; the others are collected. A root whose first
- * component is not finite matches nothing. Asynchronous; merges on one collection must
- * be ordered (one stream, or events). */
-frg_status frg_dcoll_merge(frg_dcoll* coll, const double* roots, int32_t* codes, const int32_t* keys, int64_t n,
-                           void* stream);
+ * duplicate, becomes code 6 in place; the others are collected. resid (n doubles, or
+ * NULL): a success whose residual is above resid_max (or not a number) takes no part
+ * (its code is left as it is). A root whose first component is not finite matches
+ * nothing. Asynchronous; merges on one collection must be ordered (one stream, or
+ * events). */
+frg_status frg_dcoll_merge(frg_dcoll* coll, const double* roots, int32_t* codes, const double* resid,
+                           double resid_max, const int32_t* keys, int64_t n, void* stream);
 /* Roots collected so far (synchronizes `stream`); FRG_ERR_ALLOC if a merge ran out of
  * capacity (the roots past it were marked kept but not collected). */
 frg_status frg_dcoll_size(frg_dcoll* coll, void* stream, int64_t* size);

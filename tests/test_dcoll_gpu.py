@@ -95,3 +95,28 @@ def test_device_collection_on_tracked_roots():
             assert np.array_equal(d_codes.cpu().numpy(), want)
     assert len(dc) == sum(len(c) for c in colls.values())
     dc.close()
+
+
+def test_device_collection_residual_filter():
+    """With residuals given, a success whose residual exceeds resid_max (or is NaN) takes no
+    part: it is not collected, not compared, and its code is left as it is."""
+    torch = pytest.importorskip("torch")
+    frg_build.build()
+    rng = np.random.default_rng(9)
+    n = 4000
+    roots = _batch(rng, np.zeros((0, 21), np.complex128), n)
+    codes = np.zeros(n, np.int32)
+    resid = rng.uniform(0, 2e-10, size=n)
+    resid[::97] = np.nan
+    want_codes = np.where(resid <= 1e-10, 0, 5).astype(np.int32)
+    want = _host_merge({}, roots, want_codes, np.zeros(n, np.int32))
+    dc = frg.DeviceCollection(n, TOL)
+    d_codes = torch.from_numpy(codes.copy()).cuda()
+    dc.merge(torch.from_numpy(roots.view(np.float64).copy()).cuda(), d_codes, None,
+             resid=torch.from_numpy(resid).cuda(), resid_max=1e-10)
+    got = d_codes.cpu().numpy()
+    part = resid <= 1e-10
+    assert np.array_equal(got[part], want[part])
+    assert np.all(got[~part] == 0)
+    assert len(dc) == int((want == 0).sum())
+    dc.close()
