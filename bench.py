@@ -545,7 +545,10 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "fma (fp32 + fp64 pipes)", "achieved": round(frac, 5), "peak": 1.0,
                      "unit": "fraction of the step's time the algorithmic FLOPs need at the measured FP32 and "
                              "FP64 FMA peaks: (F32/peak32 + F64/peak64)/T",
-                     "frac": round(frac, 5), "traffic": None,
+                     "frac": round(frac, 5),
+                     "traffic": round((TRAFFIC_PER_PATH["fp32_stage"] + TRAFFIC_PER_PATH["fp64_stage"]) * n),
+                     "traffic_unit": "bytes per step (both tracking stages, DRAM read + write; ncu capture of a "
+                                     "4,096-path round scaled by paths; inputs and outputs are ~1.2 KB per path)",
                      "f32_tflop": round(F32 / 1e12, 3), "f64_tflop": round(F64 / 1e12, 3),
                      "peak_fp32_tflops": round(peaks["fp32"], 2), "peak_fp64_tflops": round(peaks["fp64"], 4),
                      "peak_source": "FMA peaks of measured: bench.py's own chain-free FMA kernels (MEASURED_PEAKS.json "
@@ -566,6 +569,11 @@ def run_ours(args, rank, world):
 
 
 FRG_COUNTERS_BYTES = 48 * 8
+# DRAM bytes (read + write) per path of the two tracking stages, from one ncu capture of a
+# 4,096-path round of the chosen configuration (`bench.py --profile-case`, MemoryWorkloadAnalysis):
+# 11.67 MB for the FP32 stage and 29.85 MB for the FP64 stage; a round's traffic is taken to
+# grow in proportion to its paths
+TRAFFIC_PER_PATH = {"fp32_stage": 11.67e6 / 4096, "fp64_stage": 29.85e6 / 4096}
 
 
 # ------------------------------------------------------------------- CPU baseline
