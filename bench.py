@@ -345,7 +345,7 @@ def _timed_rounds(torch, tracker, fpm_sets, ppt, seeds, outs, depth, world, dedu
 
 
 def _collect(frg, wl, steps, outs, n):
-    """Per-task collections of K steps' device outputs."""
+    """Per-task collections of K steps' device outputs, and the outputs on the host."""
     R = outs[0].cpu().numpy().view(np.complex128)
     C = outs[1].cpu().numpy()
     E = outs[2].cpu().numpy()
@@ -353,7 +353,27 @@ def _collect(frg, wl, steps, outs, n):
     for i, s in enumerate(steps):
         sl = slice(i * n, (i + 1) * n)
         tc.merge_step(wl, s, R[sl], C[sl], E[sl])
+    tc.host = (R, C, E)
     return tc
+
+
+def _kept_root_quality(chosen, plain):
+    """Residuals of the chosen run's kept roots and, per path, the distance of its root to
+    the plain FP64 run's root of the same path (same random stream)."""
+    Rc, Cc, Ec = chosen
+    Rp, Cp, _ = plain
+    kept = (Cc == 0) & (Ec <= RESID_MAX)
+    both = kept & (Cp == 0)
+    d = np.max(np.abs(Rc[both] - Rp[both]), axis=1) / np.max(np.abs(Rp[both]), axis=1)
+    near = d <= 1e-8
+    return {"kept_roots": int(kept.sum()),
+            "kept_residual_max": float(Ec[kept].max()) if kept.any() else None,
+            "kept_residual_median": float(np.median(Ec[kept])) if kept.any() else None,
+            "successes_failing_residual": int(((Cc == 0) & ~(Ec <= RESID_MAX)).sum()),
+            "paths_kept_by_both": int(both.sum()),
+            "within_1e-8_of_fp64_track": round(float(near.mean()), 5) if both.any() else None,
+            "distance_to_fp64_track_median": float(np.median(d)) if both.any() else None,
+            "distance_to_fp64_track_p99_of_those_within": float(np.quantile(d[near], 0.99)) if near.any() else None}
 
 
 def run_ours(args, rank, world):
@@ -436,6 +456,8 @@ def run_ours(args, rank, world):
         hits += round(recall(a, c_coll.roots_of(t)) * len(a))
         found += len(a)
     rec = hits / max(found, 1)
+    quality = _kept_root_quality(c_coll.host, p_coll.host)
+    c_coll.host = p_coll.host = None
     # ---- one round of the chosen configuration with nothing else in flight: its FP32 and
     #      FP64 stages' own durations (the pipelined rounds overlap them) ----
     solo_st, _, _ = _timed_rounds(torch, chosen, d_sets[:1], ppt, seeds[:1], tuple(o[:n] for o in outs), 1, world)
@@ -539,6 +561,7 @@ def run_ours(args, rank, world):
                        "roofline_frac_fp64": round(plain_frac, 4)},
         "speedup_vs_plain_fp64": round(value / value_plain, 3),
         "recall_vs_plain_fp64": round(rec, 5),
+        "kept_root_quality": quality,
         "distinct_roots": int(distinct),
         "dedup_ms_per_step": round(c_merge_ms / k, 3),
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
