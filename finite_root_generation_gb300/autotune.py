@@ -131,7 +131,9 @@ def autotune(tasks, n=8192, rounds=2, base=None, space=None, target_recall=0.995
         return store[key]["best"]
 
     seeds = [1000 + i for i in range(rounds)]
-    ref_sets, ref_ms = _run(dict(base, precision=PREC_FP64), tasks, n, seeds, 2, device)
+    # plain FP64 with as many rounds in flight as the candidates (the largest depth searched)
+    ref_depth = max(space.get("depth", [2]))
+    ref_sets, ref_ms = _run(dict(base, precision=PREC_FP64), tasks, n, seeds, ref_depth, device)
     ref_rate = sum(len(s) for s in ref_sets) / (ref_ms * 1e-3)
     names = list(space)
     results = []
@@ -161,7 +163,7 @@ def autotune(tasks, n=8192, rounds=2, base=None, space=None, target_recall=0.995
         # re-validate the choice on fresh seeds
         fresh = [5000 + i for i in range(rounds)]
         fb = {k: v for k, v in best.items() if k != "depth"}
-        r_sets, _ = _run(dict(base, precision=PREC_FP64), tasks, n, fresh, 2, device)
+        r_sets, _ = _run(dict(base, precision=PREC_FP64), tasks, n, fresh, ref_depth, device)
         c_sets, _ = _run(dict(base, **fb), tasks, n, fresh, best["depth"], device)
         check = {"recall": _recall(r_sets, c_sets)}
         if check["recall"] < target_recall:
