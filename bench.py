@@ -272,7 +272,7 @@ def flops_per_solve():
 def _chosen_overrides(frg):
     """The chosen configuration on top of the workload's (frg.CHOSEN): mixed precision,
     the FP32 stage also running the endgame and sharpening (double-float points and
-    refinement), FP64 for steps whose condition estimate exceeds 5e5 and for finishing
+    refinement), FP64 for steps whose condition estimate exceeds 1e6 and for finishing
     every root, at most 10,000 FP64 solves per path and launch (a path still going after
     that ends as a step-limit failure; such paths crawl near a singularity and set the
     FP64 tail), paths well conditioned again carried back to FP32 in a later round, the

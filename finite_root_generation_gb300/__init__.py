@@ -61,8 +61,14 @@ class FrgConfig(ctypes.Structure):
         ("mixed_rounds", ctypes.c_int), ("lo_refine", ctypes.c_int), ("lo_endgame", ctypes.c_int),
         ("path_offset", ctypes.c_int64), ("fp64_budget", ctypes.c_int), ("lo_points", ctypes.c_int),
         ("fp64_segment", ctypes.c_int), ("handback_good", ctypes.c_int), ("lo_final", ctypes.c_int),
-        ("carry_handback", ctypes.c_int), ("round_graph", ctypes.c_int),
+        ("carry_handback", ctypes.c_int), ("round_graph", ctypes.c_int), ("system", ctypes.c_int),
     ]
+
+
+class FrgSystemDesc(ctypes.Structure):
+    """``frg_system_desc`` (include/frg_gb300.h)."""
+
+    _fields_ = [("name", ctypes.c_char * 32), ("nv", ctypes.c_int), ("np", ctypes.c_int)]
 
 
 class FrgStats(ctypes.Structure):
@@ -98,7 +104,7 @@ EXPORTS = [
     "frg_coll_save", "frg_coll_load", "frg_codes_append", "frg_lambertw0", "frg_estimate_collected",
     "frg_track_noalloc", "frg_track_rounds", "frg_set_mlp", "frg_track_features", "frg_mlp_param_count",
     "frg_mlp_grad", "frg_mlp_train", "frg_mlp_predict", "frg_dcoll_create", "frg_dcoll_destroy", "frg_dcoll_merge",
-    "frg_dcoll_size", "frg_dcoll_get",
+    "frg_dcoll_size", "frg_dcoll_get", "frg_system_info", "frg_num_systems",
 ]
 NOALLOC_MAX_TASKS = 1024
 
@@ -162,8 +168,40 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.frg_track_noalloc.argtypes = [ctypes.POINTER(FrgConfig), ctypes.c_void_p, ctypes.c_int, _I64,
                                       ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
+    lib.frg_system_info.argtypes = [ctypes.c_int, ctypes.POINTER(FrgSystemDesc)]
+    lib.frg_num_systems.restype = ctypes.c_int
     _lib = lib
     return lib
+
+
+@dataclass
+class SystemInfo:
+    id: int
+    name: str
+    nv: int   # unknowns of a root
+    np: int   # parameters of a task
+
+
+def system_info(system: int) -> SystemInfo:
+    """The system `system` tracks (0 = Stephenson II, k >= 1 = plug-in k, the modules of
+    finite_root_generation_gb300/systems in the order of systems.PLUGINS)."""
+    d = FrgSystemDesc()
+    if load().frg_system_info(int(system), ctypes.byref(d)) != 0:
+        raise FrgError(f"unknown system {system}")
+    return SystemInfo(int(system), d.name.decode(), d.nv, d.np)
+
+
+def list_systems() -> list:
+    """Every system the library was built with."""
+    return [system_info(k) for k in range(load().frg_num_systems())]
+
+
+def plugin_config(name: str, **overrides) -> FrgConfig:
+    """default_config for the plug-in system `name`: FP64 on the thread kernel."""
+    for s in list_systems():
+        if s.name == name:
+            return default_config(system=s.id, precision=PREC_FP64, kernel_variant=KERNEL_THREAD, **overrides)
+    raise FrgError(f"no system named {name}")
 
 
 def default_config(**overrides) -> FrgConfig:
@@ -180,11 +218,12 @@ def default_config(**overrides) -> FrgConfig:
 # The chosen mixed-precision setting of the benchmark: FP32 team kernel with double-float
 # points that also runs the endgame and sharpening; its corrector accepts an FP32 update
 # below 1e-6 and otherwise refines on double-float residuals to 1e-8; FP64 for steps whose
-# condition estimate exceeds 5e5 and for finishing every root, at most 10,000 FP64 solves
+# condition estimate exceeds 1e6 and for finishing every root, at most 10,000 FP64 solves
 # per path and launch; in frg_track_rounds a path well conditioned again in FP64 (32
-# solves below 5e3, or 256 FP64 solves) is carried back to FP32 in a later round, and the
-# rounds run as one CUDA graph.
-CHOSEN = dict(precision=PREC_MIXED, mixed_rounds=1, lo_endgame=1, cond_switch=5e5, lo_points=1, fp64_budget=10000,
+# solves below 1e4, or 256 FP64 solves) is carried back to FP32 in a later round, and the
+# rounds run as one CUDA graph. The fields the autotuner searches agree with its GB300
+# entry for the 128-task workload (tuned.json).
+CHOSEN = dict(precision=PREC_MIXED, mixed_rounds=1, lo_endgame=1, cond_switch=1e6, lo_points=1, fp64_budget=10000,
               lo_refine=3, newt_tol_lo=1e-6, carry_handback=1, handback_good=32, fp64_segment=256, round_graph=1)
 
 
@@ -208,7 +247,7 @@ def _ptr(a) -> int:
 
 @dataclass
 class TrackResult:
-    roots: np.ndarray       # [N, 21] complex128, canonical cognate, dehomogenized
+    roots: np.ndarray       # [N, nv] complex128, dehomogenized (Stephenson II: canonical cognate)
     codes: np.ndarray       # [N] int32
     yfinal: np.ndarray | None
     resid: np.ndarray | None
@@ -253,17 +292,27 @@ class Tracker:
         self._check(self.lib.frg_set_config(self._ctx, ctypes.byref(cfg)), "frg_set_config")
         self.config = cfg
 
+    @property
+    def dims(self):
+        """(unknowns, parameters) of the configured system."""
+        if self.config.system == 0:
+            return NV, NP
+        info = system_info(self.config.system)
+        return info.nv, info.np
+
     def track(self, fpm, paths_per_task, seed: int, want_yfinal: bool = False,
               want_resid: bool = False) -> TrackResult:
-        """Track sum(paths_per_task) paths; fpm is [ntasks, 30] complex (host)."""
-        fpm = np.ascontiguousarray(np.asarray(fpm, dtype=np.complex128).reshape(-1, NP))
+        """Track sum(paths_per_task) paths; fpm is [ntasks, np] complex (host; np = 30 for
+        Stephenson II). Roots are [N, nv], yfinal [N, nv + 2]."""
+        nv, np_ = self.dims
+        fpm = np.ascontiguousarray(np.asarray(fpm, dtype=np.complex128).reshape(-1, np_))
         ppt = np.ascontiguousarray(np.atleast_1d(np.asarray(paths_per_task, dtype=np.int64)))
         if len(ppt) != len(fpm):
             raise ValueError("paths_per_task must have one entry per task")
         n = int(ppt.sum())
-        roots = np.zeros((n, NV), np.complex128)
+        roots = np.zeros((n, nv), np.complex128)
         codes = np.zeros(n, np.int32)
-        yfinal = np.zeros((n, NY), np.complex128) if want_yfinal else None
+        yfinal = np.zeros((n, nv + 2), np.complex128) if want_yfinal else None
         resid = np.zeros(n, np.float64) if want_resid else None
         stats = FrgStats()
         st = self.lib.frg_track(self._ctx, fpm.ctypes.data, len(ppt), ppt.ctypes.data_as(_I64),

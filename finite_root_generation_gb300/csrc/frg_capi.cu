@@ -147,6 +147,7 @@ extern "C" frg_status frg_config_default(frg_config* c) {
   c->lo_final = 0;
   c->carry_handback = 0;
   c->round_graph = 0;
+  c->system = 0;
   return FRG_OK;
 }
 
@@ -177,7 +178,29 @@ frg_status frg_check_config(frg_ctx* ctx, const frg_config* c) {
     return fail(ctx, FRG_ERR_ARG, "fp64_segment and handback_good must be non-negative");
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
+  if (c->system < 0 || c->system >= frg_num_systems()) return fail(ctx, FRG_ERR_ARG, "unknown system");
+  if (c->system != 0 && (c->precision != FRG_PREC_FP64 || c->kernel_variant != FRG_KERNEL_THREAD))
+    return fail(ctx, FRG_ERR_ARG, "plug-in systems run in FP64 on the thread kernel");
   return FRG_OK;
+}
+
+extern "C" int frg_num_systems(void) { return frg_system_count(); }
+
+extern "C" frg_status frg_system_info(int system, frg_system_desc* desc) {
+  const char* name = nullptr;
+  int nv = 0, np = 0;
+  if (!desc || !frg_system_dims(system, &name, &nv, &np)) return FRG_ERR_ARG;
+  std::memset(desc, 0, sizeof(*desc));
+  std::strncpy(desc->name, name, sizeof(desc->name) - 1);
+  desc->nv = nv;
+  desc->np = np;
+  return FRG_OK;
+}
+
+// Unknowns and parameters of the configured system.
+static void dims_of(const frg_config& c, int* nv, int* np) {
+  const char* name;
+  if (!frg_system_dims(c.system, &name, nv, np)) { *nv = FRG_NV; *np = FRG_NP; }
 }
 
 extern "C" frg_status frg_create(frg_ctx** out, const frg_config* cfg, int device) {
@@ -283,6 +306,8 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
                                 uint64_t seed, cx<double>* d_roots, int32_t* d_codes, cx<double>* d_yfinal,
                                 double* d_resid, int64_t N, cudaStream_t st, cudaEvent_t* evs) {
   const bool mixed = ctx->cfg.precision == FRG_PREC_MIXED;
+  int nv, np;
+  dims_of(ctx->cfg, &nv, &np);
   std::vector<cx<double>> g;
   task_gammas(ctx->cfg, seed, ntasks, g);
   std::vector<cx<float>> g_lo(ntasks);
@@ -295,8 +320,8 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
   for (int k = 0; k < ntasks; ++k) starts[k + 1] = starts[k] + ppt[k];
   FRG_CUDA(ctx, sl.gamma.ensure(sizeof(cx<double>) * ntasks));
   FRG_CUDA(ctx, sl.gamma_lo.ensure(sizeof(cx<float>) * ntasks));
-  FRG_CUDA(ctx, sl.fpm_lo.ensure(sizeof(cx<float>) * FRG_NP * ntasks));
-  FRG_CUDA(ctx, sl.fpm_df.ensure(sizeof(cx<df>) * FRG_NP * ntasks));
+  FRG_CUDA(ctx, sl.fpm_lo.ensure(sizeof(cx<float>) * np * ntasks));
+  FRG_CUDA(ctx, sl.fpm_df.ensure(sizeof(cx<df>) * np * ntasks));
   FRG_CUDA(ctx, sl.gamma_df.ensure(sizeof(cx<df>) * ntasks));
   FRG_CUDA(ctx, sl.task_start.ensure(sizeof(int64_t) * (ntasks + 1)));
   FRG_CUDA(ctx, sl.queue.ensure(sizeof(unsigned long long) * 8));
@@ -309,8 +334,8 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
                                 cudaMemcpyHostToDevice, st));
   FRG_CUDA(ctx, cudaMemsetAsync(sl.queue.p, 0, sizeof(unsigned long long) * 8, st));
   FRG_CUDA(ctx, cudaMemsetAsync(sl.counters.p, 0, sizeof(unsigned long long) * FRG_NCOUNTERS, st));
-  FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)sl.fpm_lo.p, FRG_NP * ntasks, st));
-  FRG_CUDA(ctx, frg_launch_to_df(d_fpm, (cx<df>*)sl.fpm_df.p, FRG_NP * ntasks, st));
+  FRG_CUDA(ctx, frg_launch_to_float(d_fpm, (cx<float>*)sl.fpm_lo.p, np * ntasks, st));
+  FRG_CUDA(ctx, frg_launch_to_df(d_fpm, (cx<df>*)sl.fpm_df.p, np * ntasks, st));
 
   frg::TrackArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -357,8 +382,11 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
   }
   // persistent grids: SMs x resident blocks, capped by the work (one path per thread
   // for the thread kernels, one per 8 lanes for the team kernels)
+  int plugin_bps = 0;  // a plug-in system's kernel has its own occupancy
+  if (ctx->cfg.system != 0) FRG_CUDA(ctx, frg_track_occupancy_system(ctx->cfg.system, &plugin_bps));
   auto grid_for = [&](int mode, int64_t n) {
     int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm
+              : plugin_bps > 0           ? plugin_bps
                                          : (team ? ctx->team_blocks_per_sm[mode] : ctx->blocks_per_sm[mode]);
     int64_t grid = (int64_t)ctx->sm_count * bps;
     int64_t per_block = team ? FRG_TEAM_THREADS / 8 : FRG_TRACK_THREADS;
@@ -497,17 +525,19 @@ extern "C" frg_status frg_track(frg_ctx* ctx, const double* fpm, int ntasks, con
   if (s != FRG_OK) return s;
 
   // inputs
+  int nv, np;
+  dims_of(ctx->cfg, &nv, &np);
   const cx<double>* d_fpm = (const cx<double>*)fpm;
   if (!is_device_ptr(fpm)) {
-    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks));
-    FRG_CUDA(ctx, cudaMemcpyAsync(ctx->fpm.p, fpm, sizeof(cx<double>) * 30 * ntasks, cudaMemcpyHostToDevice, st));
+    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * np * ntasks));
+    FRG_CUDA(ctx, cudaMemcpyAsync(ctx->fpm.p, fpm, sizeof(cx<double>) * np * ntasks, cudaMemcpyHostToDevice, st));
     d_fpm = (const cx<double>*)ctx->fpm.p;
   }
   // outputs: written in place when on the device, staged otherwise
   struct Out { void* user; DevBuf* buf; size_t bytes; void* dev; bool host; };
-  Out outs[4] = {{roots, &ctx->roots, sizeof(cx<double>) * 21 * (size_t)N, nullptr, false},
+  Out outs[4] = {{roots, &ctx->roots, sizeof(cx<double>) * nv * (size_t)N, nullptr, false},
                  {codes, &ctx->codes, sizeof(int32_t) * (size_t)N, nullptr, false},
-                 {yfinal, &ctx->yfinal, sizeof(cx<double>) * 23 * (size_t)N, nullptr, false},
+                 {yfinal, &ctx->yfinal, sizeof(cx<double>) * (nv + 2) * (size_t)N, nullptr, false},
                  {resid, &ctx->resid, sizeof(double) * (size_t)N, nullptr, false}};
   for (Out& o : outs) {
     if (!o.user) continue;
@@ -772,10 +802,12 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
   }
   // the task parameters (one set, or one per round), once, before any round
   const size_t task_sets = per_round_tasks ? (size_t)nrounds : 1;
+  int nv, np;
+  dims_of(ctx->cfg, &nv, &np);
   const cx<double>* d_fpm = (const cx<double>*)fpm;
   if (!is_device_ptr(fpm)) {
-    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * FRG_NP * ntasks * task_sets));
-    FRG_CUDA(ctx, cudaMemcpy(ctx->fpm.p, fpm, sizeof(cx<double>) * FRG_NP * ntasks * task_sets,
+    FRG_CUDA(ctx, ctx->fpm.ensure(sizeof(cx<double>) * np * ntasks * task_sets));
+    FRG_CUDA(ctx, cudaMemcpy(ctx->fpm.p, fpm, sizeof(cx<double>) * np * ntasks * task_sets,
                              cudaMemcpyHostToDevice));
     d_fpm = (const cx<double>*)ctx->fpm.p;
   }
@@ -803,7 +835,7 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
   cudaEvent_t ev_start = evs.back();
   FRG_CUDA(ctx, cudaEventRecord(ev_start, ctx->slots[0]->stream));
   for (int d = 1; d < depth; ++d) FRG_CUDA(ctx, cudaStreamWaitEvent(ctx->slots[d]->stream, ev_start, 0));
-  const size_t rb = sizeof(cx<double>) * 21 * (size_t)N, cb = sizeof(int32_t) * (size_t)N,
+  const size_t rb = sizeof(cx<double>) * nv * (size_t)N, cb = sizeof(int32_t) * (size_t)N,
                eb = sizeof(double) * (size_t)N;
   const bool carry = mixed && ctx->cfg.carry_handback && ctx->cfg.kernel_variant == FRG_KERNEL_TEAM && mr == 1;
   if (carry) {
@@ -860,7 +892,7 @@ extern "C" frg_status frg_track_rounds(frg_ctx* ctx, const double* fpm, int ntas
         if (resid) { FRG_CUDA(ctx, sl.resid.ensure(eb)); d_resid = (double*)sl.resid.p; }
       }
       cudaEvent_t* rev = evs.data() + (size_t)r * (per + 1);
-      const cx<double>* fpm_r = d_fpm + (per_round_tasks ? (size_t)r * FRG_NP * ntasks : 0);
+      const cx<double>* fpm_r = d_fpm + (per_round_tasks ? (size_t)r * np * ntasks : 0);
       s = enqueue_track(ctx, sl, fpm_r, ntasks, paths_per_task, seeds[r], d_roots, d_codes, nullptr, d_resid, N, st,
                         rev);
       if (s != FRG_OK) return s;

@@ -119,14 +119,14 @@ __device__ inline void generate_start(Rng& rng, int dist, double range, cd* z /*
 // ---------------------------------------------------------------------------
 // Parameter homotopy q(t) and dq/dt (htpysupport.cu:37-62).
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int N_P = NP>
 __device__ __forceinline__ void params_at(T t, const cx<T>* spm, const cx<T>* fpm, cx<T> gamma, cx<T>* q,
                                           cx<T>* dq) {
   const cx<T> g1t = gamma * (T(1) - t);
   const cx<T> iden = cinv(g1t + cx<T>(t));
   const cx<T> gid2 = gamma * (iden * iden);
 #pragma unroll 2
-  for (int i = 0; i < NP; ++i) {
+  for (int i = 0; i < N_P; ++i) {
     const cx<T> s = spm[i], f = fpm[i];
     q[i] = (g1t * s + t * f) * iden;
     dq[i] = (f - s) * gid2;
@@ -179,19 +179,19 @@ __device__ void system_rows(const cx<T>* Y, const cx<T>* q, const cx<T>* dq, cx<
   }
 }
 
-// Scale rows [0, rows) of M (23 columns) and, if given, rhs by 1/max(|re|,|im|)
-// of the row (htpysupport.cu:259-277, :446-471).
-template <typename T>
+// Scale rows [0, rows) of M (N_Y columns, leading dimension LD) and, if given, rhs
+// by 1/max(|re|,|im|) of the row (htpysupport.cu:259-277, :446-471).
+template <typename T, int N_Y = NY, int LD = LDM>
 __device__ __forceinline__ void row_scale(cx<T>* M, int rows, cx<T>* rhs) {
 #pragma unroll 1
   for (int i = 0; i < rows; ++i) {
-    cx<T>* r = M + i * LDM;
+    cx<T>* r = M + i * LD;
     T mx = T(0);
 #pragma unroll
-    for (int c = 0; c < NY; ++c) mx = fmax(mx, fmax(tabs(r[c].re), tabs(r[c].im)));
+    for (int c = 0; c < N_Y; ++c) mx = fmax(mx, fmax(tabs(r[c].re), tabs(r[c].im)));
     const T s = T(1) / mx;
 #pragma unroll
-    for (int c = 0; c < NY; ++c) r[c] = s * r[c];
+    for (int c = 0; c < N_Y; ++c) r[c] = s * r[c];
     if (rhs) rhs[i] = s * rhs[i];
   }
 }
@@ -200,30 +200,31 @@ __device__ __forceinline__ void row_scale(cx<T>* M, int rows, cx<T>* rhs) {
 // rows [0, nelim), right-hand side b, then back substitution
 // (LinearSolve, htpysupport.cu:146-232; with nelim = 22 and x[22] = xlast fixed,
 // LinearSolveNewton, htpysupport.cu:302-400). Returns the pivot ratio
-// max|u_ii| / min|u_ii| over the eliminated rows as a condition estimate.
-template <typename T>
+// max|u_ii| / min|u_ii| over the eliminated rows as a condition estimate. N_Y x N_Y
+// with leading dimension LD (23 x 23 and 24 for Stephenson II).
+template <typename T, int N_Y = NY, int LD = LDM>
 __device__ T lu_solve(cx<T>* M, cx<T>* b, cx<T>* x, int nelim, bool fix_last, cx<T> xlast) {
   T pmax = T(0), pmin = T(-1);  // pmin < 0: no pivot seen yet
-  cx<T> ipiv[NY];
+  cx<T> ipiv[N_Y];
 #pragma unroll 1
-  for (int i = 0; i < NY; ++i) {
+  for (int i = 0; i < N_Y; ++i) {
     if (i < nelim) {
       T best = T(0);
       int br = i;
 #pragma unroll 1
       for (int k = i; k < nelim; ++k) {
-        T v = cnorm2(M[k * LDM + i]);
+        T v = cnorm2(M[k * LD + i]);
         if (v > best) { best = v; br = k; }
       }
       if (br != i) {
-        cx<T>* ri = M + i * LDM;
-        cx<T>* rb = M + br * LDM;
+        cx<T>* ri = M + i * LD;
+        cx<T>* rb = M + br * LD;
 #pragma unroll 1
-        for (int c = i; c < NY; ++c) { cx<T> tmp = ri[c]; ri[c] = rb[c]; rb[c] = tmp; }
+        for (int c = i; c < N_Y; ++c) { cx<T> tmp = ri[c]; ri[c] = rb[c]; rb[c] = tmp; }
         cx<T> tb = b[i]; b[i] = b[br]; b[br] = tb;
       }
     }
-    const cx<T>* ri = M + i * LDM;
+    const cx<T>* ri = M + i * LD;
     const cx<T> ip = cinv(ri[i]);
     ipiv[i] = ip;
     if (i < nelim) {
@@ -234,37 +235,75 @@ __device__ T lu_solve(cx<T>* M, cx<T>* b, cx<T>* x, int nelim, bool fix_last, cx
     const cx<T> bi = b[i];
 #pragma unroll 1
     for (int j = i + 1; j < nelim; ++j) {
-      cx<T>* rj = M + j * LDM;
+      cx<T>* rj = M + j * LD;
       const cx<T> l = rj[i] * ip;
 #pragma unroll 4
-      for (int c = i + 1; c < NY; ++c) rj[c] = cfms(rj[c], ri[c], l);
+      for (int c = i + 1; c < N_Y; ++c) rj[c] = cfms(rj[c], ri[c], l);
       b[j] = cfms(b[j], bi, l);
     }
   }
-  int top = NY - 1;
-  if (fix_last) { x[NY - 1] = xlast; top = NY - 2; }
+  int top = N_Y - 1;
+  if (fix_last) { x[N_Y - 1] = xlast; top = N_Y - 2; }
 #pragma unroll 1
   for (int i = top; i >= 0; --i) {
-    const cx<T>* ri = M + i * LDM;
+    const cx<T>* ri = M + i * LD;
     cx<T> sum(T(0));
 #pragma unroll 4
-    for (int c = i + 1; c < NY; ++c) sum = cfma(ri[c], x[c], sum);
+    for (int c = i + 1; c < N_Y; ++c) sum = cfma(ri[c], x[c], sum);
     x[i] = ipiv[i] * (b[i] - sum);
   }
   return pmin > T(0) ? pmax / pmin : T(1e30);
 }
 
-// SwitchPatch: rescale [Z, Z0] so that unew . [Z, Z0, t] = 1 (htpysupport.cu:9-34).
-template <typename T>
+// SwitchPatch: rescale [Z, Z0] so that unew . [Z, Z0, t] = 1 (htpysupport.cu:9-34);
+// N_Y = the path state's length (homogeneous unknowns + t).
+template <typename T, int N_Y = NY>
 __device__ __forceinline__ void switch_patch(const cx<T>* u, const cx<T>* Yold, cx<T>* Ynew) {
   cx<T> den(T(0));
 #pragma unroll 1
-  for (int i = 0; i < NZ; ++i) den = cfma(u[i], Yold[i], den);
-  const cx<T> t = Yold[NY - 1];
-  const cx<T> s = cdiv(cx<T>(T(1)) - u[NY - 1] * t, den);
+  for (int i = 0; i < N_Y - 1; ++i) den = cfma(u[i], Yold[i], den);
+  const cx<T> t = Yold[N_Y - 1];
+  const cx<T> s = cdiv(cx<T>(T(1)) - u[N_Y - 1] * t, den);
 #pragma unroll 1
-  for (int i = 0; i < NZ; ++i) Ynew[i] = s * Yold[i];
-  Ynew[NY - 1] = t;
+  for (int i = 0; i < N_Y - 1; ++i) Ynew[i] = s * Yold[i];
+  Ynew[N_Y - 1] = t;
+}
+
+// Solve the small dense system A x = b (N x N, row-major; A and b are overwritten) by
+// Gaussian elimination with partial pivoting on |a|^2, the first maximum winning: the
+// plug-in systems' start generation, which solves for the parameters that make a
+// random point an exact root.
+template <int N>
+__device__ __forceinline__ void small_solve(cd* A, cd* b, cd* x) {
+#pragma unroll 1
+  for (int i = 0; i < N; ++i) {
+    int br = i;
+    double best = cnorm2(A[i * N + i]);
+#pragma unroll 1
+    for (int k = i + 1; k < N; ++k) {
+      const double v = cnorm2(A[k * N + i]);
+      if (v > best) { best = v; br = k; }
+    }
+    if (br != i) {
+#pragma unroll 1
+      for (int c = 0; c < N; ++c) { const cd t = A[i * N + c]; A[i * N + c] = A[br * N + c]; A[br * N + c] = t; }
+      const cd t = b[i]; b[i] = b[br]; b[br] = t;
+    }
+#pragma unroll 1
+    for (int j = i + 1; j < N; ++j) {
+      const cd l = cdiv(A[j * N + i], A[i * N + i]);
+#pragma unroll 1
+      for (int c = i + 1; c < N; ++c) A[j * N + c] = A[j * N + c] - l * A[i * N + c];
+      b[j] = b[j] - l * b[i];
+    }
+  }
+#pragma unroll 1
+  for (int i = N - 1; i >= 0; --i) {
+    cd sum = b[i];
+#pragma unroll 1
+    for (int c = i + 1; c < N; ++c) sum = sum - A[i * N + c] * x[c];
+    x[i] = cdiv(sum, A[i * N + i]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -298,5 +337,23 @@ __device__ inline void canonical_cognate(const cd* r0, const cd* fpm, cd* out) {
 #pragma unroll 1
   for (int i = 0; i < NV; ++i) out[i] = swap ? r1[i] : r0[i];
 }
+
+// The Stephenson II system as the tracker's system type (the other systems are the
+// generated plug-ins of frg_plugins_gen.cuh, with the same members): rows of the
+// homotopy Jacobian and F, the start (GenerateStart), the canonical root (cognates).
+struct SysStephenson2 {
+  static constexpr int ID = 0;
+  static constexpr int NV = frg::NV;
+  static constexpr int NP = frg::NP;
+  template <typename T, int LD>
+  __device__ static void rows(const cx<T>* Y, const cx<T>* q, const cx<T>* dq, cx<T>* M, cx<T>* F) {
+    static_assert(LD == LDM, "Stephenson II rows are laid out with leading dimension LDM");
+    system_rows<T>(Y, q, dq, M, F);
+  }
+  __device__ static void start(Rng& rng, int dist, double range, cd* z, cd* q) {
+    generate_start(rng, dist, range, z, q);
+  }
+  __device__ static void canonical(const cd* root, const cd* fpm, cd* out) { canonical_cognate(root, fpm, out); }
+};
 
 }  // namespace frg

@@ -91,6 +91,12 @@ cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cu
 cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);
 cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream);
+// Occupancy of the FP64 thread kernel of `system` (0 = Stephenson II, k = plug-in k).
+cudaError_t frg_track_occupancy_system(int system, int* blocks_per_sm);
+// Name, unknowns and parameters of `system`; 0 for an unknown id. Host only.
+int frg_system_dims(int system, const char** name, int* nv, int* np);
+// Number of systems: Stephenson II and the generated plug-ins.
+int frg_system_count();
 // Validates a run configuration (every field frg_create and frg_set_config accept);
 // ctx may be null, otherwise it receives the error text.
 frg_status frg_check_config(frg_ctx* ctx, const frg_config* c);

@@ -114,6 +114,7 @@ extern "C" frg_status frg_track_noalloc(const frg_config* cfg, const double* fpm
   // modes), before any GPU work
   if (frg_check_config(nullptr, cfg) != FRG_OK) return FRG_ERR_ARG;
   if (cfg->precision != FRG_PREC_FP64) return FRG_ERR_ARG;  // mixed precision needs per-path buffers
+  if (cfg->system != 0) return FRG_ERR_ARG;                 // its scratch holds Stephenson II tasks
   NoallocTasks tk;  // the set-up kernel's launch parameter, built on the host stack
   NoallocTasks* tp = &tk;
   tp->ntasks = ntasks;

@@ -29,15 +29,45 @@ def distinct_roots(roots, codes, resid=None, resid_max=1e-10, dup_tol=1e-6):
     return coll.roots()
 
 
+def distinct_rows(roots, keep=None, dup_tol=1e-6):
+    """Distinct rows of `roots` ([n, nv] complex, any nv: the plug-in systems' roots),
+    among those with `keep` true, by the collection's duplicate rule (every real
+    component within dup_tol); the first of a group of duplicates in Re(root[0]) order
+    stays. Returns [k, nv] sorted by Re(root[0])."""
+    r = np.asarray(roots, np.complex128)
+    r = r.reshape(len(r), -1) if r.size else r.reshape(0, max(r.shape[-1] if r.ndim == 2 else 1, 1))
+    if keep is not None:
+        r = r[np.asarray(keep, bool)]
+    r = r[np.all(np.isfinite(r), axis=1)]
+    r = r[np.argsort(r[:, 0].real, kind="stable")]
+    parts = np.concatenate([r.real, r.imag], axis=1)
+    kept = []
+    for i in range(len(r)):
+        dup = False
+        for j in reversed(kept):
+            if parts[i, 0] - parts[j, 0] > dup_tol:
+                break
+            if np.max(np.abs(parts[i] - parts[j])) <= dup_tol:
+                dup = True
+                break
+        if not dup:
+            kept.append(i)
+    return r[kept]
+
+
 def recall(reference_roots, found_roots, rtol=1e-8):
-    """Fraction of `reference_roots` present in `found_roots` (both [k, 21]).
+    """Fraction of `reference_roots` present in `found_roots` (both [k, nv]; nv = 21 for
+    Stephenson II, a plug-in system's unknowns otherwise).
 
     Roots with a non-finite component never match. Candidates are found by a binary
     search on the first component's real part, so the cost is O((n + m) log m) plus
     the candidates inside each tolerance window, each window checked vectorised.
     """
-    a = np.asarray(reference_roots, np.complex128).reshape(-1, 21)
-    b = np.asarray(found_roots, np.complex128).reshape(-1, 21)
+    a = np.asarray(reference_roots, np.complex128)
+    b = np.asarray(found_roots, np.complex128)
+    nv = a.shape[-1] if a.ndim == 2 else (b.shape[-1] if b.ndim == 2 else 21)
+    a = a.reshape(-1, nv)
+    b = b.reshape(-1, nv)
     if len(a) == 0:
         return 1.0
     b = b[np.all(np.isfinite(b), axis=1)]

@@ -123,7 +123,21 @@ typedef struct frg_config {
   int round_graph;       /* frg_track_rounds with carry_handback: 1 = every round's launches, on
                             every stream, are captured into one CUDA graph and launched once (the
                             same results); 0 = launched one by one */
+  int system;            /* the polynomial system tracked: 0 = Stephenson II (the reference's
+                            htpykinematics.cu, nV = 21, nP = 30); k >= 1 = generated plug-in k
+                            (frg_system_info). A plug-in runs the FP64 thread kernel
+                            (precision FP64, kernel_variant THREAD) through frg_track,
+                            frg_track_async and frg_track_rounds; its tasks are ntasks x np
+                            parameters, its roots N x nv, its yfinal N x (nv + 2), and its roots
+                            are reported as tracked (no cognate map) */
 } frg_config;
+
+/* A system the library tracks (frg_config.system). */
+typedef struct frg_system_desc {
+  char name[32];         /* "stephenson2" for system 0, the plug-in module's NAME otherwise */
+  int nv;                /* unknowns of a root (affine) */
+  int np;                /* parameters of a task */
+} frg_system_desc;
 
 /* Per-call counters (all paths of the call). */
 typedef struct frg_stats {
@@ -159,6 +173,13 @@ typedef struct frg_ctx frg_ctx;
 
 /* Fill cfg with the reference's defaults. */
 frg_status frg_config_default(frg_config* cfg);
+
+/* Describe system `system` (0 = Stephenson II, 1..frg_num_systems()-1 = the generated
+ * plug-ins); FRG_ERR_ARG for an unknown id. The reference hard-wires one system
+ * (nV = 21, nP = 30, htpykinematics.cuh:8-9); this replaces those constants. Host only,
+ * no GPU needed. */
+frg_status frg_system_info(int system, frg_system_desc* desc);
+int frg_num_systems(void);
 
 /* Create a context on CUDA device `device` (replaces the reference's implicit
  * device 0 and its cudaMalloc block, frg.cu:139, :201-236). */

@@ -337,41 +337,77 @@ void or_jpar(const double* Z, const double* q, double* out) {
 /* Homotopy support (htpysupport.cu).                                          */
 /* ------------------------------------------------------------------------- */
 
+/* The tracked system: Stephenson II (p NULL; nv 21, np 30) or a generated plug-in.
+ * The path state is Y = [Z (nv), Z0, t] (ny = nv + 2 entries), H has nz = nv + 1
+ * rows, and the tracker's matrices are ny x ny, row-major with stride ny. */
+typedef struct or_plugin or_plugin;
+typedef struct { int nv, np; const or_plugin* p; } osys;
+static const osys STEPH = {OR_NV, OR_NP, NULL};
+#define NY_(S) ((S)->nv + 2)
+#define NZ_(S) ((S)->nv + 1)
+
 /* q(t) = (gamma (1-t) spm + t fpm) / (gamma (1-t) + t)   (htpysupport.cu:37-48) */
-void or_q(double t, const double* spm, const double* fpm, const double* gamma, double* out) {
+static void q_s(const osys* S, double t, const double* spm, const double* fpm, const double* gamma, double* out) {
   cd g = mk(gamma[0], gamma[1]);
   cd g1t = cmul(g, mk(1.0 - t, 0));
   cd den = cadd(g1t, mk(t, 0));
-  for (int i = 0; i < OR_NP; ++i)
+  for (int i = 0; i < S->np; ++i)
     st(out, i, cdiv(cadd(cmul(g1t, ld(spm, i)), cmul(mk(t, 0), ld(fpm, i))), den));
+}
+void or_q(double t, const double* spm, const double* fpm, const double* gamma, double* out) {
+  q_s(&STEPH, t, spm, fpm, gamma, out);
 }
 
 /* dq/dt = gamma (fpm - spm) / (gamma (1-t) + t)^2   (htpysupport.cu:51-62) */
-void or_dqdt(double t, const double* spm, const double* fpm, const double* gamma, double* out) {
+static void dqdt_s(const osys* S, double t, const double* spm, const double* fpm, const double* gamma,
+                   double* out) {
   cd g = mk(gamma[0], gamma[1]);
   cd den = cadd(cmul(g, mk(1.0 - t, 0)), mk(t, 0));
   den = cmul(den, den);
-  for (int i = 0; i < OR_NP; ++i) st(out, i, cdiv(cmul(csub(ld(fpm, i), ld(spm, i)), g), den));
+  for (int i = 0; i < S->np; ++i) st(out, i, cdiv(cmul(csub(ld(fpm, i), ld(spm, i)), g), den));
 }
+void or_dqdt(double t, const double* spm, const double* fpm, const double* gamma, double* out) {
+  dqdt_s(&STEPH, t, spm, fpm, gamma, out);
+}
+
+static void plugin_rows(const osys* S, const double* Y, const double* q, const double* dq, double* M,
+                        double* F);
 
 /* H = [F(Z; q(t)); u . Y - 1]   (htpysupport.cu:64-86) */
+static void h_s(const osys* S, const double* Y, const double* u, const double* spm, const double* fpm,
+                const double* gamma, double* out) {
+  double q[2 * OR_NP];
+  const int ny = NY_(S);
+  q_s(S, Y[2 * (ny - 1)], spm, fpm, gamma, q);
+  if (S->p) {
+    double M[2 * OR_NY * OR_NY], dq[2 * OR_NP];
+    memset(dq, 0, sizeof(dq));
+    plugin_rows(S, Y, q, dq, M, out);
+  } else {
+    or_fsys(Y, q, out);
+  }
+  cd d = mk(0, 0);
+  for (int i = 0; i < ny; ++i) d = cadd(d, cmul(ld(u, i), ld(Y, i)));
+  st(out, S->nv, csub(d, mk(1, 0)));
+}
 void or_h(const double* Y, const double* u, const double* spm, const double* fpm,
           const double* gamma, double* out) {
-  double q[2 * OR_NP];
-  or_q(Y[2 * 22], spm, fpm, gamma, q);
-  or_fsys(Y, q, out);
-  cd d = mk(0, 0);
-  for (int i = 0; i < OR_NY; ++i) d = cadd(d, cmul(ld(u, i), ld(Y, i)));
-  st(out, 21, csub(d, mk(1, 0)));
+  h_s(&STEPH, Y, u, spm, fpm, gamma, out);
 }
 
-/* JH = [dF/dZ | dF/dq . dq/dt ; u], 22 x 23 row-major   (htpysupport.cu:89-144) */
-void or_jh(const double* Y, const double* u, const double* spm, const double* fpm,
-           const double* gamma, double* out) {
+/* JH = [dF/dZ | dF/dq . dq/dt ; u], nz x ny row-major   (htpysupport.cu:89-144) */
+static void jh_s(const osys* S, const double* Y, const double* u, const double* spm, const double* fpm,
+                 const double* gamma, double* out) {
   double q[2 * OR_NP], dq[2 * OR_NP];
-  double t = Y[2 * 22];
-  or_q(t, spm, fpm, gamma, q);
-  or_dqdt(t, spm, fpm, gamma, dq);
+  const int ny = NY_(S);
+  double t = Y[2 * (ny - 1)];
+  q_s(S, t, spm, fpm, gamma, q);
+  dqdt_s(S, t, spm, fpm, gamma, dq);
+  if (S->p) {
+    plugin_rows(S, Y, q, dq, out, NULL);
+    for (int c = 0; c < ny; ++c) st(out, S->nv * ny + c, ld(u, c));
+    return;
+  }
   links L; unpack_links(Y, &L);
   for (int j = 1; j <= 7; ++j) {
     cd f[3], dZ[3][22], dP[3][6];
@@ -386,23 +422,30 @@ void or_jh(const double* Y, const double* u, const double* spm, const double* fp
   }
   for (int c = 0; c < OR_NY; ++c) st(out, 21 * 23 + c, ld(u, c));
 }
+void or_jh(const double* Y, const double* u, const double* spm, const double* fpm,
+           const double* gamma, double* out) {
+  jh_s(&STEPH, Y, u, spm, fpm, gamma, out);
+}
 
 /* SwitchPatch: rescale Z so that unew . [Z, t] = 1   (htpysupport.cu:9-34) */
-void or_switch_patch(const double* u, const double* Yold, double* Ynew) {
+static void switch_patch_s(const osys* S, const double* u, const double* Yold, double* Ynew) {
+  const int nz = NZ_(S);
   cd den = mk(0, 0);
-  for (int i = 0; i < 22; ++i) den = cadd(den, cmul(ld(u, i), ld(Yold, i)));
-  cd t = ld(Yold, 22);
-  cd s = cdiv(csub(mk(1, 0), cmul(ld(u, 22), t)), den);
-  for (int i = 0; i < 22; ++i) st(Ynew, i, cmul(s, ld(Yold, i)));
-  st(Ynew, 22, t);
+  for (int i = 0; i < nz; ++i) den = cadd(den, cmul(ld(u, i), ld(Yold, i)));
+  cd t = ld(Yold, nz);
+  cd s = cdiv(csub(mk(1, 0), cmul(ld(u, nz), t)), den);
+  for (int i = 0; i < nz; ++i) st(Ynew, i, cmul(s, ld(Yold, i)));
+  st(Ynew, nz, t);
+}
+void or_switch_patch(const double* u, const double* Yold, double* Ynew) {
+  switch_patch_s(&STEPH, u, Yold, Ynew);
 }
 
 /* Dense LU with partial pivoting on |a|^2 (first maximum wins), rows swapped by
  * pointer, then back substitution   (htpysupport.cu:146-232). nelim = number of
  * rows that take part (23 for the tangent solve; 22 for Newton, whose last unknown
  * is fixed to xlast, htpysupport.cu:302-400). */
-static void lu_solve(cd* mat, cd* b, cd* x, int nelim, int fix_last, cd xlast) {
-  const int n = OR_NY;
+static void lu_solve(int n, cd* mat, cd* b, cd* x, int nelim, int fix_last, cd xlast) {
   cd* a[OR_NY];
   for (int i = 0; i < n; ++i) a[i] = mat + i * n;
   for (int i = 0; i < n; ++i) {
@@ -431,21 +474,21 @@ static void lu_solve(cd* mat, cd* b, cd* x, int nelim, int fix_last, cd xlast) {
 }
 
 void or_linear_solve(double* mat, double* b, double* x) {
-  lu_solve((cd*)mat, (cd*)b, (cd*)x, OR_NY, 0, mk(0, 0));
+  lu_solve(OR_NY, (cd*)mat, (cd*)b, (cd*)x, OR_NY, 0, mk(0, 0));
 }
 
 /* Scale each of the first `rows` rows by 1/max(|re|,|im|) of that row
  * (htpysupport.cu:259-277 and :446-471). */
-static void row_scale(cd* m, int rows, cd* h) {
+static void row_scale(int ny, cd* m, int rows, cd* h) {
   for (int i = 0; i < rows; ++i) {
     double mx = 0.0;
-    for (int j = 0; j < OR_NY; ++j) {
-      if (fabs(m[i * OR_NY + j].re) > mx) mx = fabs(m[i * OR_NY + j].re);
-      if (fabs(m[i * OR_NY + j].im) > mx) mx = fabs(m[i * OR_NY + j].im);
+    for (int j = 0; j < ny; ++j) {
+      if (fabs(m[i * ny + j].re) > mx) mx = fabs(m[i * ny + j].re);
+      if (fabs(m[i * ny + j].im) > mx) mx = fabs(m[i * ny + j].im);
     }
     double s = 1.0 / mx;
     if (h) h[i] = cscal(s, h[i]);
-    for (int j = 0; j < OR_NY; ++j) m[i * OR_NY + j] = cscal(s, m[i * OR_NY + j]);
+    for (int j = 0; j < ny; ++j) m[i * ny + j] = cscal(s, m[i * ny + j]);
   }
 }
 
@@ -457,24 +500,29 @@ static double vnorm(const cd* v, int n) {
 
 /* IVP: tangent dY/ds from [JH; Vc] dY = e_23, normalised to unit length with
  * real dt/ds (arclength) or to dt = 1 (t-stepping)   (htpysupport.cu:237-299). */
-void or_ivp(int tstepQ, const double* Yc, const double* Vc, const double* u, const double* spm,
-            const double* fpm, const double* gamma, double* out) {
+static void ivp_s(const osys* S, int tstepQ, const double* Yc, const double* Vc, const double* u,
+                  const double* spm, const double* fpm, const double* gamma, double* out) {
+  const int ny = NY_(S), nz = NZ_(S);
   cd M[OR_NY * OR_NY], b[OR_NY], x[OR_NY];
-  or_jh(Yc, u, spm, fpm, gamma, (double*)M);
-  for (int j = 0; j < OR_NY; ++j) M[22 * OR_NY + j] = ld(Vc, j);
-  row_scale(M, 22, NULL);
-  for (int i = 0; i < OR_NY; ++i) b[i] = mk(0, 0);
-  b[22] = mk(1, 0);
-  lu_solve(M, b, x, OR_NY, 0, mk(0, 0));
+  jh_s(S, Yc, u, spm, fpm, gamma, (double*)M);
+  for (int j = 0; j < ny; ++j) M[nz * ny + j] = ld(Vc, j);
+  row_scale(ny, M, nz, NULL);
+  for (int i = 0; i < ny; ++i) b[i] = mk(0, 0);
+  b[nz] = mk(1, 0);
+  lu_solve(ny, M, b, x, ny, 0, mk(0, 0));
   cd sc;
   if (!tstepQ) {
-    double th = atan2(x[22].im, x[22].re);
-    sc = cmul(mk(cos(th), -sin(th)), mk(1.0 / vnorm(x, OR_NY), 0));
+    double th = atan2(x[nz].im, x[nz].re);
+    sc = cmul(mk(cos(th), -sin(th)), mk(1.0 / vnorm(x, ny), 0));
   } else {
-    sc = cinv(x[22]);
+    sc = cinv(x[nz]);
   }
-  for (int i = 0; i < OR_NY; ++i) st(out, i, cmul(sc, x[i]));
-  out[2 * 22 + 1] = 0.0;
+  for (int i = 0; i < ny; ++i) st(out, i, cmul(sc, x[i]));
+  out[2 * nz + 1] = 0.0;
+}
+void or_ivp(int tstepQ, const double* Yc, const double* Vc, const double* u, const double* spm,
+            const double* fpm, const double* gamma, double* out) {
+  ivp_s(&STEPH, tstepQ, Yc, Vc, u, spm, fpm, gamma, out);
 }
 
 /* Dormand-Prince 6(5), 8 stages; stage i's velocity patch is k_{i-1}
@@ -496,8 +544,8 @@ static const double DP_B[8] = {61. / 864., 0., 98415. / 321776., 16807. / 146016
 
 /* sum_{i<n} w[i] s k[i], accumulated from the last term to the first as the
  * reference's nested .add() chains do. */
-static void comb(double s, const double* w, cd k[8][OR_NY], int n, cd* out) {
-  for (int e = 0; e < OR_NY; ++e) {
+static void comb(int ny, double s, const double* w, cd k[8][OR_NY], int n, cd* out) {
+  for (int e = 0; e < ny; ++e) {
     cd acc = mk(0, 0);
     int first = 1;
     for (int i = n - 1; i >= 0; --i) {
@@ -510,49 +558,56 @@ static void comb(double s, const double* w, cd k[8][OR_NY], int n, cd* out) {
   }
 }
 
-void or_dp65(double s, double tol, int tstepQ, const double* Yc, const double* Vc, const double* u,
-             const double* spm, const double* fpm, const double* gamma, double* Yn, double* Vn,
-             double* err, double* scale) {
+static void dp65_s(const osys* S, double s, double tol, int tstepQ, const double* Yc, const double* Vc,
+                   const double* u, const double* spm, const double* fpm, const double* gamma, double* Yn,
+                   double* Vn, double* err, double* scale) {
+  const int ny = NY_(S);
   cd k[8][OR_NY];
   cd Yarg[OR_NY], d[OR_NY];
-  or_ivp(tstepQ, Yc, Vc, u, spm, fpm, gamma, (double*)k[0]);
+  ivp_s(S, tstepQ, Yc, Vc, u, spm, fpm, gamma, (double*)k[0]);
   for (int stg = 1; stg < 8; ++stg) {
-    comb(s, DP_A[stg], k, stg, d);
-    for (int e = 0; e < OR_NY; ++e) Yarg[e] = cadd(ld(Yc, e), d[e]);
-    or_ivp(tstepQ, (double*)Yarg, (double*)k[stg - 1], u, spm, fpm, gamma, (double*)k[stg]);
+    comb(ny, s, DP_A[stg], k, stg, d);
+    for (int e = 0; e < ny; ++e) Yarg[e] = cadd(ld(Yc, e), d[e]);
+    ivp_s(S, tstepQ, (double*)Yarg, (double*)k[stg - 1], u, spm, fpm, gamma, (double*)k[stg]);
   }
-  comb(s, DP_E, k, 8, d);
-  *err = vnorm(d, OR_NY);
+  comb(ny, s, DP_E, k, 8, d);
+  *err = vnorm(d, ny);
   if (*err > 10e-17) *scale = 0.8 * pow(tol / (*err), 1. / 6.);
   else *scale = 5.0;
   if (*scale > 5) *scale = 5;
-  comb(s, DP_B, k, 8, d);
-  for (int e = 0; e < OR_NY; ++e) st(Yn, e, cadd(ld(Yc, e), d[e]));
-  memcpy(Vn, k[7], sizeof(cd) * OR_NY);
+  comb(ny, s, DP_B, k, 8, d);
+  for (int e = 0; e < ny; ++e) st(Yn, e, cadd(ld(Yc, e), d[e]));
+  memcpy(Vn, k[7], sizeof(cd) * ny);
+}
+void or_dp65(double s, double tol, int tstepQ, const double* Yc, const double* Vc, const double* u,
+             const double* spm, const double* fpm, const double* gamma, double* Yn, double* Vn,
+             double* err, double* scale) {
+  dp65_s(&STEPH, s, tol, tstepQ, Yc, Vc, u, spm, fpm, gamma, Yn, Vn, err, scale);
 }
 
 /* Newton corrector with t fixed at tgoal, row-scaled J and H   (htpysupport.cu:407-494) */
-static int newton_impl(double tgoal, const double* Vn, const double* u, const double* spm,
+static int newton_impl(const osys* S, double tgoal, const double* Vn, const double* u, const double* spm,
                        const double* fpm, const double* gamma, int maxIts, double tol,
                        int residualtype, double* YN, double* residual) {
+  const int ny = NY_(S), nz = NZ_(S);
   int i = 0;
   *residual = 100.0;
   while (i < maxIts && *residual > tol) {
-    cd M[OR_NY * OR_NY], h[22], bb[22 + 1], dY[OR_NY];
-    or_jh(YN, u, spm, fpm, gamma, (double*)M);
-    for (int j = 0; j < OR_NY; ++j) M[22 * OR_NY + j] = ld(Vn, j);
-    or_h(YN, u, spm, fpm, gamma, (double*)h);
-    row_scale(M, 22, h);
-    double tdiff = tgoal - YN[2 * 22];
-    for (int j = 0; j < 22; ++j) bb[j] = cscal(-1.0, h[j]);
-    bb[22] = mk(0, 0);
-    lu_solve(M, bb, dY, 22, 1, mk(tdiff, 0));
-    for (int e = 0; e < OR_NY; ++e) st(YN, e, cadd(ld(YN, e), dY[e]));
+    cd M[OR_NY * OR_NY], h[OR_NY], bb[OR_NY], dY[OR_NY];
+    jh_s(S, YN, u, spm, fpm, gamma, (double*)M);
+    for (int j = 0; j < ny; ++j) M[nz * ny + j] = ld(Vn, j);
+    h_s(S, YN, u, spm, fpm, gamma, (double*)h);
+    row_scale(ny, M, nz, h);
+    double tdiff = tgoal - YN[2 * nz];
+    for (int j = 0; j < nz; ++j) bb[j] = cscal(-1.0, h[j]);
+    bb[nz] = mk(0, 0);
+    lu_solve(ny, M, bb, dY, nz, 1, mk(tdiff, 0));
+    for (int e = 0; e < ny; ++e) st(YN, e, cadd(ld(YN, e), dY[e]));
     if (residualtype == 0) {
-      or_h(YN, u, spm, fpm, gamma, (double*)h);
-      *residual = vnorm(h, 22);
+      h_s(S, YN, u, spm, fpm, gamma, (double*)h);
+      *residual = vnorm(h, nz);
     } else {
-      *residual = vnorm(dY, OR_NY);
+      *residual = vnorm(dY, ny);
     }
     i++;
   }
@@ -562,7 +617,7 @@ static int newton_impl(double tgoal, const double* Vn, const double* u, const do
 void or_newton(double tgoal, const double* Vn, const double* u, const double* spm, const double* fpm,
                const double* gamma, int maxIts, double tol, int residualtype, double* YN,
                double* residual) {
-  newton_impl(tgoal, Vn, u, spm, fpm, gamma, maxIts, tol, residualtype, YN, residual);
+  newton_impl(&STEPH, tgoal, Vn, u, spm, fpm, gamma, maxIts, tol, residualtype, YN, residual);
 }
 
 /* Raw Philox block and uniform draw, exported for the known-answer tests. */
@@ -641,29 +696,31 @@ void or_generate_start(const or_config* c, uint64_t seed, uint64_t stream, doubl
 /* The path tracker (htpytrack.cu:33-220).                                     */
 /* ------------------------------------------------------------------------- */
 
-static void draw_patch(const or_config* c, rng_t* r, double* u) {
+static void draw_patch(int ny, const or_config* c, rng_t* r, double* u) {
   double R = c->patch_range;
-  for (int i = 0; i < OR_NY; ++i) {
+  for (int i = 0; i < ny; ++i) {
     u[2 * i] = 2.0 * R * urand(r) - R;
     u[2 * i + 1] = 2.0 * R * urand(r) - R;
   }
 }
 
-void or_track_path(const or_config* c, const double* spt, const double* spm, const double* fpm,
-                   const double* gamma, uint64_t seed, uint64_t stream, double* Yfinal, int* code,
-                   or_stats* stt) {
+static void track_path_s(const osys* sys, const or_config* c, const double* spt, const double* spm,
+                         const double* fpm, const double* gamma, uint64_t seed, uint64_t stream,
+                         double* Yfinal, int* code, or_stats* stt) {
+  const int nv = sys->nv, ny = NY_(sys), it = ny - 1; /* it: index of t in the path state */
   rng_t rng = {seed, stream, 0};  /* the reference hands TrackPath a fresh copy of the state */
   double Vc[2 * OR_NY], Yn[2 * OR_NY], Vn[2 * OR_NY], YN[2 * OR_NY], u[2 * OR_NY];
   double* Yc = Yfinal;            /* htpytrack.cu:46: the working point lives in Yfinal */
   or_stats local; memset(&local, 0, sizeof(local));
   or_stats* S = stt ? stt : &local;
-  memmove(Yc, spt, sizeof(double) * 2 * 21);
-  Yc[2 * 21] = 1.0; Yc[2 * 21 + 1] = 0.0;
-  Yc[2 * 22] = 0.0; Yc[2 * 22 + 1] = 0.0;
-  draw_patch(c, &rng, u);
-  or_switch_patch(u, Yc, Yc);
-  draw_patch(c, &rng, Vc);
-  or_ivp(0, Yc, Vc, u, spm, fpm, gamma, Vc);
+  const size_t ybytes = sizeof(double) * 2 * ny;
+  memmove(Yc, spt, sizeof(double) * 2 * nv);
+  Yc[2 * nv] = 1.0; Yc[2 * nv + 1] = 0.0;
+  Yc[2 * it] = 0.0; Yc[2 * it + 1] = 0.0;
+  draw_patch(ny, c, &rng, u);
+  switch_patch_s(sys, u, Yc, Yc);
+  draw_patch(ny, c, &rng, Vc);
+  ivp_s(sys, 0, Yc, Vc, u, spm, fpm, gamma, Vc);
   S->ivp_solves++;
 
   double s = c->s_init, err = 0, scale = 0, residual = 100.0;
@@ -675,7 +732,7 @@ void or_track_path(const or_config* c, const double* spt, const double* spm, con
     for (;;) { /* correction loop */
       for (;;) { /* final steps loop */
         for (;;) { /* predictor loop */
-          or_dp65(s, c->rk_tol, tstepQ, Yc, Vc, u, spm, fpm, gamma, Yn, Vn, &err, &scale);
+          dp65_s(sys, s, c->rk_tol, tstepQ, Yc, Vc, u, spm, fpm, gamma, Yn, Vn, &err, &scale);
           S->rk_attempts++; S->ivp_solves += 8;
           if (ministep++ == c->max_ministeps) { *code = 2; return; }
           if (err <= c->rk_tol) break;
@@ -684,22 +741,22 @@ void or_track_path(const or_config* c, const double* spt, const double* spm, con
           if (s < c->s_min) s = c->s_min * 0.9;
           streak = 0;
         }
-        if (Yn[2 * 22] <= 1. - c->nudge_trigger) break;
-        if (fabs(1. - Yn[2 * 22]) < c->sharp_trigger) break;
+        if (Yn[2 * it] <= 1. - c->nudge_trigger) break;
+        if (fabs(1. - Yn[2 * it]) < c->sharp_trigger) break;
         tstepQ = 1;
-        s = 1 - Yc[2 * 22];
+        s = 1 - Yc[2 * it];
       }
-      if (fabs(1. - Yn[2 * 22]) < c->sharp_trigger) break;
+      if (fabs(1. - Yn[2 * it]) < c->sharp_trigger) break;
       int i = 0;
       while (i < c->newt_attempts) {
-        memcpy(YN, Yn, sizeof(YN));
-        S->newton_iters += newton_impl(Yn[2 * 22], Vn, u, spm, fpm, gamma, c->newt_its, c->newt_tol,
+        memcpy(YN, Yn, ybytes);
+        S->newton_iters += newton_impl(sys, Yn[2 * it], Vn, u, spm, fpm, gamma, c->newt_its, c->newt_tol,
                                        c->newt_residual, YN, &residual);
         S->newton_calls++;
         if (ministep++ == c->max_ministeps) { *code = 2; return; }
         if (residual < c->newt_tol) break;
-        draw_patch(c, &rng, u);
-        or_switch_patch(u, Yn, Yn);
+        draw_patch(ny, c, &rng, u);
+        switch_patch_s(sys, u, Yn, Yn);
         i++;
       }
       if (residual < c->newt_tol) break;
@@ -708,9 +765,9 @@ void or_track_path(const or_config* c, const double* spt, const double* spm, con
       if (s < c->s_min) s = c->s_min * 0.9;
       streak = 0;
     }
-    if (fabs(1. - Yn[2 * 22]) < c->sharp_trigger) break;
-    memcpy(Yc, YN, sizeof(YN));
-    memcpy(Vc, Vn, sizeof(Vc));
+    if (fabs(1. - Yn[2 * it]) < c->sharp_trigger) break;
+    memcpy(Yc, YN, ybytes);
+    memcpy(Vc, Vn, ybytes);
     streak++;
     if (streak < c->caution_steps && scale > 1.) scale = 1.;
     s *= scale;
@@ -722,17 +779,180 @@ void or_track_path(const or_config* c, const double* spt, const double* spm, con
   /* sharpening at t = 1 (htpytrack.cu:194-216) */
   int i = 0;
   while (i < c->sharp_attempts) {
-    memcpy(Yfinal, Yn, sizeof(Yn));
-    S->newton_iters += newton_impl(1., Vn, u, spm, fpm, gamma, c->sharp_its, c->sharp_tol,
+    memcpy(Yfinal, Yn, ybytes);
+    S->newton_iters += newton_impl(sys, 1., Vn, u, spm, fpm, gamma, c->sharp_its, c->sharp_tol,
                                    c->sharp_residual, Yfinal, &residual);
     S->newton_calls++;
     if (ministep++ == c->max_ministeps) { *code = 2; return; }
     if (residual < c->sharp_tol) break;
-    draw_patch(c, &rng, u);
-    or_switch_patch(u, Yn, Yn);
+    draw_patch(ny, c, &rng, u);
+    switch_patch_s(sys, u, Yn, Yn);
     i++;
   }
   if (residual >= c->sharp_tol) *code = 5;
+}
+
+void or_track_path(const or_config* c, const double* spt, const double* spm, const double* fpm,
+                   const double* gamma, uint64_t seed, uint64_t stream, double* Yfinal, int* code,
+                   or_stats* stt) {
+  track_path_s(&STEPH, c, spt, spm, fpm, gamma, seed, stream, Yfinal, code, stt);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Plug-in systems: the generated rows and starts of the modules in            */
+/* finite_root_generation_gb300/systems (frg_plugins_gen.h).                   */
+/* ------------------------------------------------------------------------- */
+
+/* A x = b (n x n, row-major; A and b overwritten): Gaussian elimination with partial
+ * pivoting on |a|^2, the first maximum winning, for the start parameters. */
+static void small_solve(int n, cd* A, cd* b, cd* x) {
+  for (int i = 0; i < n; ++i) {
+    int br = i;
+    double best = cnorm2(A[i * n + i]);
+    for (int k = i + 1; k < n; ++k) {
+      double v = cnorm2(A[k * n + i]);
+      if (v > best) { best = v; br = k; }
+    }
+    if (br != i) {
+      for (int c = 0; c < n; ++c) { cd t = A[i * n + c]; A[i * n + c] = A[br * n + c]; A[br * n + c] = t; }
+      cd t = b[i]; b[i] = b[br]; b[br] = t;
+    }
+    for (int j = i + 1; j < n; ++j) {
+      cd l = cdiv(A[j * n + i], A[i * n + i]);
+      for (int c = i + 1; c < n; ++c) A[j * n + c] = csub(A[j * n + c], cmul(l, A[i * n + c]));
+      b[j] = csub(b[j], cmul(l, b[i]));
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    cd sum = b[i];
+    for (int c = i + 1; c < n; ++c) sum = csub(sum, cmul(A[i * n + c], x[c]));
+    x[i] = cdiv(sum, A[i * n + i]);
+  }
+}
+
+struct or_plugin {
+  int id;
+  const char* name;
+  int nv, np;
+  /* rows 0..nv-1 of JH into M (stride ld): dF/dZ, dF/dZ0, the t column; F if given */
+  void (*rows)(const cd* Y, const cd* q, const cd* dq, cd* M, int ld, cd* F);
+  /* start root z and start parameters q from the random stream r */
+  void (*start)(const or_config* c, rng_t* r, cd* z, cd* q);
+};
+
+#include "frg_plugins_gen.h"
+
+static void plugin_rows(const osys* S, const double* Y, const double* q, const double* dq, double* M,
+                        double* F) {
+  S->p->rows((const cd*)Y, (const cd*)q, (const cd*)dq, (cd*)M, NY_(S), (cd*)F);
+}
+
+static int plugin_sys(int system, osys* out) {
+  for (int k = 0; k < OR_NUM_PLUGINS; ++k)
+    if (OR_PLUGINS[k].id == system) {
+      out->nv = OR_PLUGINS[k].nv;
+      out->np = OR_PLUGINS[k].np;
+      out->p = &OR_PLUGINS[k];
+      return 1;
+    }
+  return 0;
+}
+
+int or_num_plugins(void) { return OR_NUM_PLUGINS; }
+
+int or_plugin_info(int system, int* nv, int* np) {
+  osys S;
+  if (!plugin_sys(system, &S)) return 0;
+  *nv = S.nv;
+  *np = S.np;
+  return 1;
+}
+
+int or_plugin_rows(int system, const double* Y, const double* q, const double* dq, double* M, double* F) {
+  osys S;
+  if (!plugin_sys(system, &S)) return 0;
+  plugin_rows(&S, Y, q, dq, M, F);
+  return 1;
+}
+
+int or_plugin_start(int system, const or_config* c, uint64_t seed, uint64_t stream, double* spt, double* spm) {
+  osys S;
+  if (!plugin_sys(system, &S)) return 0;
+  rng_t r = {seed, stream, 0};
+  S.p->start(c, &r, (cd*)spt, (cd*)spm);
+  return 1;
+}
+
+/* One plug-in path: start, track, dehomogenize (the root as tracked), and the
+ * row-scaled residual max_i |F_i| / max_c |dF_i/dZ_c| of the target system at the root. */
+static void plugin_path(const osys* S, const or_config* c, uint64_t seed, uint64_t stream, const double* fpm,
+                        const double* gamma, double* root, int* code, double* Yfinal, double* resid) {
+  const int nv = S->nv, ny = NY_(S), nz = NZ_(S);
+  double spt[2 * OR_NV], spm[2 * OR_NP], Y[2 * OR_NY], u[2 * OR_NY];
+  rng_t r = {seed, stream, 0};
+  S->p->start(c, &r, (cd*)spt, (cd*)spm);
+  track_path_s(S, c, spt, spm, fpm, gamma, seed, stream, Y, code, NULL);
+  if (Yfinal) memcpy(Yfinal, Y, sizeof(double) * 2 * ny);
+  memset(u, 0, sizeof(u));
+  u[2 * nv] = 1.0;
+  switch_patch_s(S, u, Y, Y);
+  memcpy(root, Y, sizeof(double) * 2 * nv);
+  if (resid) {
+    double Yr[2 * OR_NY], dq[2 * OR_NP], M[2 * OR_NY * OR_NY], F[2 * OR_NY];
+    memcpy(Yr, Y, sizeof(double) * 2 * nv);
+    Yr[2 * nv] = 1.0; Yr[2 * nv + 1] = 0.0;
+    Yr[2 * (nv + 1)] = 1.0; Yr[2 * (nv + 1) + 1] = 0.0;
+    memset(dq, 0, sizeof(dq));
+    plugin_rows(S, Yr, fpm, dq, M, F);
+    double rmax = 0.0;
+    for (int i = 0; i < nv; ++i) {
+      double mx = 0.0;
+      for (int e = 0; e < nz; ++e) {
+        mx = fmax(mx, fabs(M[2 * (i * ny + e)]));
+        mx = fmax(mx, fabs(M[2 * (i * ny + e) + 1]));
+      }
+      double ri = sqrt(F[2 * i] * F[2 * i] + F[2 * i + 1] * F[2 * i + 1]) / mx;
+      rmax = (ri == ri) ? fmax(rmax, ri) : INFINITY;
+    }
+    *resid = rmax;
+  }
+}
+
+typedef struct {
+  const osys* S; const or_config* c; uint64_t seed; const uint64_t* streams; int64_t n; int ntasks;
+  const int64_t* task_start; const double* fpm; const double* gamma; double* roots; int* codes;
+  double* yfinal; double* resid; int nthreads; int w;
+} plugin_arg;
+
+static void* plugin_worker(void* p) {
+  plugin_arg* a = (plugin_arg*)p;
+  const int nv = a->S->nv, ny = NY_(a->S), np = a->S->np;
+  for (int64_t i = a->w; i < a->n; i += a->nthreads) {
+    int k = 0;
+    while (k + 1 < a->ntasks && a->task_start[k + 1] <= i) ++k;
+    plugin_path(a->S, a->c, a->seed, a->streams[i], a->fpm + 2 * np * k, a->gamma + 2 * k, a->roots + 2 * nv * i,
+                a->codes + i, a->yfinal ? a->yfinal + 2 * ny * i : NULL, a->resid ? a->resid + i : NULL);
+  }
+  return NULL;
+}
+
+int or_plugin_batch(int system, const or_config* c, uint64_t seed, const uint64_t* streams, int64_t n, int ntasks,
+                    const int64_t* task_start, const double* fpm, const double* gamma, double* roots, int* codes,
+                    double* yfinal, double* resid, int nthreads) {
+  osys S;
+  if (!plugin_sys(system, &S)) return 0;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  plugin_arg args[256];
+  for (int w = 0; w < nthreads; ++w) {
+    plugin_arg a = {&S, c, seed, streams, n, ntasks, task_start, fpm, gamma, roots, codes, yfinal, resid,
+                    nthreads, w};
+    args[w] = a;
+    pthread_create(&th[w], NULL, plugin_worker, &args[w]);
+  }
+  for (int w = 0; w < nthreads; ++w) pthread_join(th[w], NULL);
+  return 1;
 }
 
 /* ------------------------------------------------------------------------- */

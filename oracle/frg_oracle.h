@@ -77,6 +77,22 @@ void or_homotopy_batch(const or_config* c, uint64_t seed, const uint64_t* stream
 int64_t or_sort_merge(const double* coll, int64_t ncoll, const double* fpt, int* codes, int64_t n,
                       double tol, double* coll_out);
 double or_lambertw0(double z);
+
+/* Plug-in systems (finite_root_generation_gb300/systems; system ids 1..): the same
+ * tracker on the generated rows and starts. Each returns 0 for an unknown system.
+ *   or_plugin_rows   M: nv x (nv + 2) rows of JH, row-major (dF/dZ, dF/dZ0, t column);
+ *                    F: nv values (optional)
+ *   or_plugin_batch  paths i = 0..n-1 with random streams streams[i]; path i belongs to the
+ *                    task k with task_start[k] <= i < task_start[k + 1] (ntasks + 1 entries);
+ *                    fpm ntasks x np, gamma ntasks; roots n x nv (as tracked, dehomogenized),
+ *                    yfinal n x (nv + 2) (optional), resid n (optional, row-scaled residual) */
+int or_num_plugins(void);
+int or_plugin_info(int system, int* nv, int* np);
+int or_plugin_rows(int system, const double* Y, const double* q, const double* dq, double* M, double* F);
+int or_plugin_start(int system, const or_config* c, uint64_t seed, uint64_t stream, double* spt, double* spm);
+int or_plugin_batch(int system, const or_config* c, uint64_t seed, const uint64_t* streams, int64_t n, int ntasks,
+                    const int64_t* task_start, const double* fpm, const double* gamma, double* roots, int* codes,
+                    double* yfinal, double* resid, int nthreads);
 void or_philox_block(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 double or_uniform01(uint64_t seed, uint64_t stream, uint64_t index);
 

@@ -236,6 +236,54 @@ class Oracle:
                                    ctypes.c_int64(len(fpt)), ctypes.c_double(tol), _p(out))
         return out[:m], codes
 
+    # ---- plug-in systems (frg_plugins_gen.h; system ids 1..) ----
+    def plugin_info(self, system):
+        """(nv, np) of plug-in `system`; raises KeyError for an unknown id."""
+        nv, np_ = ctypes.c_int(), ctypes.c_int()
+        if not self.lib.or_plugin_info(int(system), ctypes.byref(nv), ctypes.byref(np_)):
+            raise KeyError(system)
+        return nv.value, np_.value
+
+    def plugin_rows(self, system, Y, q, dq):
+        """(M [nv, nv + 2], F [nv]): rows of the homotopy Jacobian and F at Y = [Z, Z0, t]."""
+        nv, _ = self.plugin_info(system)
+        M = np.zeros((nv, nv + 2), np.complex128)
+        F = np.zeros(nv, np.complex128)
+        self.lib.or_plugin_rows(int(system), _p(_c(Y)), _p(_c(q)), _p(_c(dq)), _p(M), _p(F))
+        return M, F
+
+    def plugin_start(self, system, seed, stream, cfg: OrConfig | None = None):
+        cfg = cfg or self.config()
+        nv, np_ = self.plugin_info(system)
+        spt = np.zeros(nv, np.complex128)
+        spm = np.zeros(np_, np.complex128)
+        self.lib.or_plugin_start(int(system), ctypes.byref(cfg), ctypes.c_uint64(seed), ctypes.c_uint64(stream),
+                                 _p(spt), _p(spm))
+        return spt, spm
+
+    def plugin_batch(self, system, fpm, gammas, seed, paths_per_task, cfg: OrConfig | None = None, nthreads=None,
+                     want_yfinal=False, path_offset=0):
+        """Track sum(paths_per_task) paths of plug-in `system`: path i uses random stream
+        path_offset + i and belongs to task k (fpm [ntasks, np], gammas [ntasks]);
+        returns (roots [n, nv], codes [n], resid [n], yfinal [n, nv + 2] or None)."""
+        cfg = cfg or self.config()
+        nv, np_ = self.plugin_info(system)
+        fpm = _c(fpm).reshape(-1, np_)
+        ppt = np.atleast_1d(np.asarray(paths_per_task, np.int64))
+        starts = np.ascontiguousarray(np.concatenate([[0], np.cumsum(ppt)]).astype(np.int64))
+        n = int(starts[-1])
+        streams = np.ascontiguousarray(np.arange(n, dtype=np.uint64) + np.uint64(path_offset))
+        roots = np.zeros((n, nv), np.complex128)
+        codes = np.zeros(n, np.int32)
+        resid = np.zeros(n)
+        yf = np.zeros((n, nv + 2), np.complex128) if want_yfinal else None
+        nthreads = nthreads or os.cpu_count() or 1
+        self.lib.or_plugin_batch(int(system), ctypes.byref(cfg), ctypes.c_uint64(seed), streams.ctypes.data_as(_U64),
+                                 ctypes.c_int64(n), ctypes.c_int(len(ppt)), starts.ctypes.data_as(_I64), _p(fpm),
+                                 _p(_c(gammas)), _p(roots), codes.ctypes.data_as(_I),
+                                 _p(yf) if yf is not None else None, _p(resid), ctypes.c_int(nthreads))
+        return roots, codes, resid, yf
+
     def lambertw0(self, z):
         return self.lib.or_lambertw0(float(z))
 

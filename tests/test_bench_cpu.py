@@ -38,3 +38,18 @@ def test_kept_root_quality_summary():
     assert q["kept_roots"] == 3 and q["successes_failing_residual"] == 1
     assert q["kept_residual_max"] <= 1e-10
     assert q["paths_kept_by_both"] == 3 and abs(q["within_1e-8_of_fp64_track"] - 2 / 3) < 1e-4
+
+
+def test_chosen_setting_is_the_tuned_one():
+    """The benchmark applies frg.CHOSEN, then the autotuner's table entry for the GPU;
+    the GPU parity tests run frg.CHOSEN. Every field the table sets agrees with CHOSEN,
+    so the tested setting is the measured one."""
+    import finite_root_generation_gb300 as frg
+    from finite_root_generation_gb300 import autotune
+
+    tuned = autotune.tuned_setting("NVIDIA GB300", "c5")
+    assert tuned is not None
+    tuned.pop("depth")
+    cfg = frg.chosen_config()
+    for key, v in tuned.items():
+        assert getattr(cfg, key) == v, key

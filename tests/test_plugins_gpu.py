@@ -1,0 +1,89 @@
+"""System plug-ins on the GPU: the CUDA thread kernel instantiated on the generated
+systems against the oracle's tracker on the same random streams, path for path, and the
+plug-ins' known answers.
+
+Bars: codes equal on >= 99 % of the paths; where both succeed, roots within 1e-8
+relative on >= 99 % of the paths (the oracle and the kernel round differently: FMA
+contraction and the order of the complex products); every successful root's row-scaled
+FP64 residual <= 1e-10 but at most 1e-3 of them; the known roots found.
+"""
+import numpy as np
+import pytest
+
+import finite_root_generation_gb300 as frg
+from finite_root_generation_gb300 import build as frg_build
+from finite_root_generation_gb300.metrics import distinct_rows
+from finite_root_generation_gb300.systems import burmester5, conic2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    frg_build.build()
+
+
+def _gammas(oracle, seed, ntasks):
+    """The library's random gamma of each task of a call with `seed`."""
+    phi = 2 * np.pi * np.array([oracle.uniform01(seed, 2**64 - 1 - k, 0) for k in range(ntasks)])
+    return np.exp(1j * phi)
+
+
+def _compare(oracle, name, tasks, ppt, seed, start_dist):
+    cfg = frg.plugin_config(name, start_dist=start_dist, gamma_mode=frg.GAMMA_RANDOM)
+    sid = cfg.system
+    with frg.Tracker(cfg) as t:
+        res = t.track(tasks, ppt, seed, want_resid=True)
+    o_roots, o_codes, o_resid, _ = oracle.plugin_batch(sid, tasks, _gammas(oracle, seed, len(ppt)), seed, ppt,
+                                                       cfg=oracle.config(start_dist=start_dist))
+    agree = np.mean(res.codes == o_codes)
+    both = (res.codes == 0) & (o_codes == 0)
+    rel = np.max(np.abs(res.roots[both] - o_roots[both]), axis=1) / np.max(np.abs(o_roots[both]), axis=1)
+    ok = res.codes == 0
+    bad = int(np.sum(~(res.resid[ok] <= 1e-10)))
+    print(f"{name}: {len(res.codes)} paths, codes agree {agree:.4f}, {both.sum()} both succeed, "
+          f"{np.mean(rel <= 1e-8):.4f} within 1e-8 (max {rel.max():.2e}), {bad} above the residual bar, "
+          f"track {res.stats['track_ms']:.1f} ms")
+    assert agree >= 0.99
+    assert np.mean(rel <= 1e-8) >= 0.99
+    assert bad <= 1e-3 * ok.sum()
+    return res, o_roots, o_codes
+
+
+@pytest.mark.parametrize("start_dist", [frg.START_UNIFORM, frg.START_NORMAL])
+def test_conic2_matches_oracle_and_known_roots(oracle, start_dist):
+    rng = np.random.default_rng(21)
+    q_known, known = conic2.line_pair_task(rng.normal(size=4) + 1j * rng.normal(size=4),
+                                           rng.normal(size=4) + 1j * rng.normal(size=4))
+    q_rand = rng.normal(size=12) + 1j * rng.normal(size=12)
+    tasks = np.stack([q_known, q_rand])
+    res, _, _ = _compare(oracle, "conic2", tasks, [512, 512], 5, start_dist)
+    ok = res.codes[:512] == 0
+    found = distinct_rows(res.roots[:512], ok)
+    assert len(found) == 4
+    for r in found:
+        assert np.min(np.max(np.abs(known - r), axis=1)) <= 1e-10
+
+
+def test_burmester5_matches_oracle_and_finds_four_dyads(oracle):
+    tasks = np.stack([burmester5.physical_task(np.random.default_rng(s)) for s in (5, 6)])
+    res, _, _ = _compare(oracle, "burmester5", tasks, [2048, 2048], 17, frg.START_NORMAL)
+    for k in range(2):
+        sl = slice(2048 * k, 2048 * (k + 1))
+        dyads = distinct_rows(res.roots[sl], (res.codes[sl] == 0) & (res.resid[sl] <= 1e-10))
+        assert len(dyads) == 4, dyads
+
+
+def test_plugin_rounds_match_single_calls():
+    """frg_track_rounds on a plug-in: each round equals frg_track with that round's seed."""
+    cfg = frg.plugin_config("burmester5", start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM)
+    task = burmester5.physical_task(np.random.default_rng(9))
+    n, seeds = 1024, [3, 4, 5]
+    roots = np.zeros((len(seeds) * n, 5), np.complex128)
+    codes = np.zeros(len(seeds) * n, np.int32)
+    with frg.Tracker(cfg) as t:
+        t.track_rounds(task, [n], seeds, roots, codes, depth=2)
+        for r, s in enumerate(seeds):
+            single = t.track(task, [n], s)
+            assert np.array_equal(codes[r * n:(r + 1) * n], single.codes)
+            assert np.array_equal(roots[r * n:(r + 1) * n], single.roots)
