@@ -548,10 +548,10 @@ def run_ours(args, rank, world):
                    "setting_from": "autotuner table (finite_root_generation_gb300/tuned.json)" if tuned
                                    else "frg.CHOSEN",
                    "chosen": "mixed precision: FP32 team kernel (double-float points and refinement, endgame and "
-                             "sharpening included), FP64 team kernel for steps with condition estimate > 5e5 "
-                             "(at most 10,000 FP64 solves per path and launch) and for finishing; paths well "
-                             "conditioned again carried back to FP32 in a later round; rounds as one CUDA graph; "
-                             "duplicate removal on the device",
+                             "sharpening included), FP64 team kernel for steps with condition estimate > "
+                             f"{chosen_cfg.cond_switch:.0e} (at most {chosen_cfg.fp64_budget:,} FP64 solves per "
+                             "path and launch) and for finishing; paths well conditioned again carried back to "
+                             "FP32 in a later round; rounds as one CUDA graph; duplicate removal on the device",
                    "l2": f"not flushed: per-round state (start values 816 B, hand-off record 1.2 KB, outputs "
                          f"348 B per path: ~{n * 2364 / 1e6:.0f} MB per round, {depth} rounds in flight) exceeds "
                          "the 129 MB L2",
