@@ -686,6 +686,134 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ------------------------------------------------------------------ plug-in systems
+def _plugin_tasks(name, ntasks):
+    """Seeded tasks of a plug-in system: five physical positions (burmester5) or two line
+    pairs in general position (conic2), task k from seed k."""
+    import importlib
+    mod = importlib.import_module(f"finite_root_generation_gb300.systems.{name}")
+    out = []
+    for k in range(ntasks):
+        rng = np.random.default_rng(k)
+        if name == "burmester5":
+            out.append(mod.physical_task(rng))
+        elif name == "conic2":
+            out.append(mod.line_pair_task(rng.normal(size=4) + 1j * rng.normal(size=4),
+                                          rng.normal(size=4) + 1j * rng.normal(size=4))[0])
+        else:
+            raise SystemExit(f"no benchmark tasks for system {name}")
+    return np.stack(out)
+
+
+def plugin_flops_per_solve(name, nv, np_):
+    """Algorithmic FLOPs of one linear-system step of the thread kernel on a plug-in
+    system (complex mul = 6, add = 2, real x complex = 2, FMA = 8, reciprocal = 12):
+    q(t), dq/dt (np x 24), the generated rows (their operation counts, in the header),
+    row scaling (nz x ny x 2), dense LU of the ny x ny system with its right-hand side
+    (sum over pivots of a reciprocal and, per row below, a multiplier and ny - 1 - i
+    FMAs plus one for the right-hand side), back substitution and the tangent's norm.
+    The tangent step is counted for Newton steps as well (one row fewer eliminated)."""
+    import re
+    gen = open(os.path.join(ROOT, "finite_root_generation_gb300", "csrc", "frg_plugins_gen.cuh")).read()
+    i = gen.index(f"struct Sys_{name} ")
+    m = re.search(r"ROWS_CMUL = (\d+), ROWS_CADD = (\d+), ROWS_SMUL = (\d+)", gen[i:])
+    cm, ca, sm = (int(x) for x in m.groups())
+    ny, nz = nv + 2, nv + 1
+    f = np_ * 24 + 6 * cm + 2 * ca + 2 * sm + nz * ny * 2
+    f += sum(12 + (ny - 1 - i) * (6 + 8 * (ny - 1 - i) + 8) for i in range(ny))
+    f += sum(8 * (ny - 1 - i) + 6 for i in range(ny))
+    f += ny * 10
+    return f
+
+
+def run_plugin(args):
+    """--system NAME: paths/s of a plug-in system on the FP64 thread kernel, rounds of
+    --plugin-tasks tasks x --plugin-paths paths through frg_track_rounds (device outputs,
+    CUDA-event span), end to end from host buffers, the kernel's FP64 roofline, and the
+    oracle's tracker on the host cores (no reference implementation exists for a plug-in)."""
+    import torch
+
+    import finite_root_generation_gb300 as frg
+    from finite_root_generation_gb300 import build as frg_build
+    from finite_root_generation_gb300.metrics import distinct_rows
+
+    frg_build.build()
+    cfg = frg.plugin_config(args.system, start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM)
+    info = frg.system_info(cfg.system)
+    T, n, k, depth = args.plugin_tasks, args.plugin_paths, args.steps, 2
+    tasks = _plugin_tasks(args.system, T)
+    N = T * n
+    dev = torch.device("cuda", 0)
+    fpm_d = torch.from_numpy(tasks.view(np.float64).copy()).to(dev)
+    seeds = [SEED_BASE + s for s in range(k)]
+    roots = torch.empty((k * N, info.nv, 2), dtype=torch.float64, device=dev)
+    codes = torch.empty(k * N, dtype=torch.int32, device=dev)
+    resid = torch.empty(k * N, dtype=torch.float64, device=dev)
+    with frg.Tracker(cfg) as t:
+        for w in range(args.warmup):
+            t.track_rounds(fpm_d, [n] * T, [WARM_SEED_BASE + w], roots[:N], codes[:N], resid[:N], depth=1)
+        torch.cuda.synchronize()
+        with ClockSampler() as clk:
+            st = t.track_rounds(fpm_d, [n] * T, seeds, roots, codes, resid, depth=depth)
+        torch.cuda.synchronize()
+        # end to end: host task set in, host roots, codes and residuals out
+        h_roots = np.zeros((k * N, info.nv), np.complex128)
+        h_codes = np.zeros(k * N, np.int32)
+        h_resid = np.zeros(k * N)
+        t0 = time.perf_counter()
+        t.track_rounds(tasks, [n] * T, seeds, h_roots, h_codes, h_resid, depth=depth)
+        e2e_s = time.perf_counter() - t0
+    ms = st["track_ms"]
+    r = roots.cpu().numpy().view(np.complex128).reshape(k * N, info.nv)
+    c = codes.cpu().numpy()
+    e = resid.cpu().numpy()
+    assert np.array_equal(c, h_codes) and np.array_equal(r, h_roots), "device and host runs differ"
+    distinct = []
+    for j in range(T):
+        sel = np.concatenate([np.arange(s * N + j * n, s * N + (j + 1) * n) for s in range(k)])
+        distinct.append(len(distinct_rows(r[sel], (c[sel] == 0) & (e[sel] <= RESID_MAX))))
+    solves = st["ivp_solves"] + st["newton_iters"]
+    fps = plugin_flops_per_solve(args.system, info.nv, info.np)
+    peaks = measure_fma_peaks()
+    achieved = solves * fps / (ms * 1e-3) / 1e12
+    value = k * N / (ms * 1e-3)
+    line = {"metric": f"paths tracked/s, plug-in system {args.system} (FP64)", "value": round(value, 1),
+            "unit": "paths/s", "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": round(ms / k, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded tasks and start points)",
+            "config": {"workload": f"{args.system}: {T} tasks x {n} paths per step ({info.nv} unknowns, "
+                                   f"{info.np} parameters), complex-normal starts, random gamma per task and step, "
+                                   f"{depth} rounds in flight",
+                       "paths_per_step": N, "l2": "not flushed: per-step outputs and state are small; the "
+                                                  "kernel is compute bound"},
+            "codes": [int(x) for x in np.bincount(c, minlength=8)],
+            "distinct_roots_per_task": {"min": min(distinct), "max": max(distinct)},
+            "e2e": {"value": round(k * N / e2e_s, 1), "unit": "paths/s",
+                    "h2d_bytes_per_step": int(tasks.nbytes), "d2h_bytes_per_step": int(N * (info.nv * 16 + 12))},
+            "roofline": {"bound": "fp64", "achieved": round(achieved, 4), "peak": round(peaks["fp64"], 4),
+                         "unit": "TFLOP/s", "frac": round(achieved / peaks["fp64"], 4), "traffic": None,
+                         "flops_per_solve": fps, "solves": int(solves),
+                         "peak_source": "of measured: bench.py's own FP64 FMA kernel"},
+            "gpu_launches": 3 * k, "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        o = oracle.Oracle()
+        m = min(n, args.cpu_paths)
+        gam = [_gamma_of(o.uniform01, seeds[0], j) for j in range(T)]
+        ppt = [m] * T
+        t0 = time.perf_counter()
+        o_roots, o_codes, _, _ = o.plugin_batch(cfg.system, tasks, gam, seeds[0], ppt,
+                                                cfg=o.config(start_dist=1))
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": round(m * T / dt, 1), "unit": "paths/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": f"first {m} paths of each task of step 0 "
+                                                          f"({m * T} paths) by the oracle's tracker, {dt:.2f} s"}
+    return line
+
+
 def run_profile_case(args):
     """The ncu target: one round of the chosen configuration (or plain FP64 with
     --profile-plain) on --profile-paths paths of the workload's first two tasks, one
@@ -723,9 +851,15 @@ def main():
                     help="one chosen-configuration round on --profile-paths paths (an ncu target), nothing else")
     ap.add_argument("--profile-paths", type=int, default=4096)
     ap.add_argument("--profile-plain", action="store_true", help="with --profile-case: plain FP64 instead")
+    ap.add_argument("--system", default=None, help="measure a plug-in system (its own JSON line) instead")
+    ap.add_argument("--plugin-tasks", type=int, default=64)
+    ap.add_argument("--plugin-paths", type=int, default=4096)
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
+        return
+    if args.system:
+        print(json.dumps(run_plugin(args)))
         return
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("need --steps >= 1 and --warmup >= 0")

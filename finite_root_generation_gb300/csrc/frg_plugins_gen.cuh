@@ -12,11 +12,13 @@
 namespace frg {
 
 // ---- system 1: conic2 (2 unknowns, 12 parameters)
+// rows(): 48 complex mul, 32 complex add/sub, 3 real x complex
 struct Sys_conic2 {
   static constexpr int ID = 1;
   static constexpr int NV = 2;
   static constexpr int NP = 12;
   static constexpr int NS = 2;
+  static constexpr int ROWS_CMUL = 48, ROWS_CADD = 32, ROWS_SMUL = 3;
   template <typename T, int LD>
   __device__ static void rows(const cx<T>* Y, const cx<T>* q, const cx<T>* dq, cx<T>* M, cx<T>* F) {
     const cx<T> u_x = Y[0];
@@ -120,11 +122,13 @@ struct Sys_conic2 {
 };
 
 // ---- system 2: burmester5 (5 unknowns, 20 parameters)
+// rows(): 158 complex mul, 101 complex add/sub, 5 real x complex
 struct Sys_burmester5 {
   static constexpr int ID = 2;
   static constexpr int NV = 5;
   static constexpr int NP = 20;
   static constexpr int NS = 5;
+  static constexpr int ROWS_CMUL = 158, ROWS_CADD = 101, ROWS_SMUL = 5;
   template <typename T, int LD>
   __device__ static void rows(const cx<T>* Y, const cx<T>* q, const cx<T>* dq, cx<T>* M, cx<T>* F) {
     const cx<T> u_G = Y[0];

@@ -149,6 +149,30 @@ def cse_block(exprs, tmp_prefix):
     return repl, reduced
 
 
+def count_ops(exprs):
+    """(complex multiplications, complex additions, real-scalar multiplications) of the
+    straight-line code for `exprs` (powers as repeated products)."""
+    cm = ca = sm = 0
+    for e in exprs:
+        for node in sp.preorder_traversal(e):
+            if isinstance(node, sp.Mul):
+                coeff, rest = node.as_coeff_Mul()
+                cm += max(len(sp.Mul.make_args(rest)) - 1, 0)
+                sm += 1 if coeff not in (1, -1) else 0
+            elif isinstance(node, sp.Add):
+                ca += len(node.args) - 1
+            elif isinstance(node, sp.Pow):
+                cm += int(node.exp) - 1
+    return cm, ca, sm
+
+
+def rows_cost(info):
+    """Operation counts of one rows() evaluation (Jacobian rows, t column and F)."""
+    flat = [e for row in info["jac"] for e in row] + info["Fh"]
+    repl, red = cse_block(flat, "r_")
+    return count_ops([e for _, e in repl] + list(red))
+
+
 def emit_rows(mod, info, dialect):
     """Body lines of rows(): loads, CSE temporaries, the row entries and F."""
     names = names_for(info)
@@ -246,12 +270,15 @@ def emit_start(mod, info, dialect):
 
 def cuda_struct(mod, info, sid):
     cname = "Sys_" + mod.NAME
+    cm, ca, sm = rows_cost(info)
     out = [f"// ---- system {sid}: {mod.NAME} ({info['nv']} unknowns, {info['np']} parameters)",
+           f"// rows(): {cm} complex mul, {ca} complex add/sub, {sm} real x complex",
            f"struct {cname} {{",
            f"  static constexpr int ID = {sid};",
            f"  static constexpr int NV = {info['nv']};",
            f"  static constexpr int NP = {info['np']};",
            f"  static constexpr int NS = {info['ns']};",
+           f"  static constexpr int ROWS_CMUL = {cm}, ROWS_CADD = {ca}, ROWS_SMUL = {sm};",
            "  template <typename T, int LD>",
            "  __device__ static void rows(const cx<T>* Y, const cx<T>* q, const cx<T>* dq, cx<T>* M, cx<T>* F) {"]
     out += ["  " + ln for ln in emit_rows(mod, info, "cuda")]
