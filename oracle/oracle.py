@@ -223,8 +223,8 @@ class Oracle:
             f = np.abs(self.fsys(Z, q))
             J = self.jvar(Z, q)
             m = np.maximum(np.abs(J.real), np.abs(J.imag)).max(axis=1)
-            q = f / m
-            out[i] = np.inf if np.any(np.isnan(q)) else np.max(q)
+            ratio = f / m
+            out[i] = np.inf if np.any(np.isnan(ratio)) else np.max(ratio)
         return out
 
     def sort_merge(self, coll, fpt, codes, tol=1e-6):

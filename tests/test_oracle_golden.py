@@ -1,5 +1,7 @@
 """Pin the C restatement of the reference (the oracle) against golden vectors
 recorded from the reference's own sources (tests/golden/make_golden.py)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -129,6 +131,22 @@ def test_full_paths_match_reference(oracle, golden):
     for i in range(n):
         if want_codes[i] == 0:
             assert rel_err(roots[i], golden["path_roots"][i]) < 1e-8
+
+
+def test_batch_residuals_are_per_root(oracle, golden):
+    """Residuals of many roots in one call equal the roots' residuals one at a time (and,
+    where the reference's host build exists, the reference's own FSYS/JVAR residuals)."""
+    roots = golden["path_roots"][golden["path_codes"] == 0]
+    batch = oracle.residuals(roots, T_REF)
+    single = np.array([oracle.residuals(r[None], T_REF)[0] for r in roots])
+    assert len(roots) > 10
+    assert np.array_equal(batch, single)
+    assert np.all(batch < 1e-10)
+    import oracle as oracle_mod
+    if os.path.exists(oracle_mod.REF_SO):
+        ref = oracle_mod.RefLib().residuals(roots, T_REF)
+        # both are round-off (~1e-16) at these roots; they agree to that level
+        np.testing.assert_allclose(batch, ref, rtol=0, atol=1e-13)
 
 
 def test_cognate_matches_reference(oracle, golden):
