@@ -738,7 +738,7 @@ def run_plugin(args):
     from finite_root_generation_gb300.metrics import distinct_rows
 
     frg_build.build()
-    cfg = frg.plugin_config(args.system, start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM)
+    cfg = frg.plugin_config(args.system, start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=INF_TOL)
     info = frg.system_info(cfg.system)
     T, n, k, depth = args.plugin_tasks, args.plugin_paths, args.steps, 2
     tasks = _plugin_tasks(args.system, T)

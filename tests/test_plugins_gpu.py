@@ -5,7 +5,10 @@ plug-ins' known answers.
 Bars: codes equal on >= 99 % of the paths; where both succeed, roots within 1e-8
 relative on >= 99 % of the paths (the oracle and the kernel round differently: FMA
 contraction and the order of the complex products); every successful root's row-scaled
-FP64 residual <= 1e-10 but at most 1e-3 of them; the known roots found.
+FP64 residual <= 1e-10 but at most 1e-3 of them; the known roots found. Endpoints with
+|Z0| < 1e-8 max|Z| are infinite roots (code 7; the oracle's endpoints classified by the
+same rule): burmester5's physical tasks have solutions at infinity, which sharpening
+reaches in homogeneous coordinates (|Z0| / max|Z| ~ 1e-34) and which are no finite roots.
 """
 import numpy as np
 import pytest
@@ -29,13 +32,19 @@ def _gammas(oracle, seed, ntasks):
     return np.exp(1j * phi)
 
 
+INF_TOL = 1e-8
+
+
 def _compare(oracle, name, tasks, ppt, seed, start_dist):
-    cfg = frg.plugin_config(name, start_dist=start_dist, gamma_mode=frg.GAMMA_RANDOM)
+    cfg = frg.plugin_config(name, start_dist=start_dist, gamma_mode=frg.GAMMA_RANDOM, inf_tol=INF_TOL)
     sid = cfg.system
     with frg.Tracker(cfg) as t:
         res = t.track(tasks, ppt, seed, want_resid=True)
-    o_roots, o_codes, o_resid, _ = oracle.plugin_batch(sid, tasks, _gammas(oracle, seed, len(ppt)), seed, ppt,
-                                                       cfg=oracle.config(start_dist=start_dist))
+    o_roots, o_codes, o_resid, o_yf = oracle.plugin_batch(sid, tasks, _gammas(oracle, seed, len(ppt)), seed, ppt,
+                                                          cfg=oracle.config(start_dist=start_dist), want_yfinal=True)
+    nv = o_roots.shape[1]
+    at_inf = np.abs(o_yf[:, nv]) < INF_TOL * np.max(np.abs(o_yf[:, :nv]), axis=1)
+    o_codes = np.where((o_codes == 0) & at_inf, 7, o_codes)
     agree = np.mean(res.codes == o_codes)
     both = (res.codes == 0) & (o_codes == 0)
     rel = np.max(np.abs(res.roots[both] - o_roots[both]), axis=1) / np.max(np.abs(o_roots[both]), axis=1)
