@@ -192,11 +192,12 @@ frg_status frg_set_config(frg_ctx* ctx, const frg_config* cfg);
  * frg.cu:30-124, :361-404). Path i of task k uses random stream
  * (sum of paths of earlier tasks) + i of `seed`; the reference's per-thread curand
  * subsequence i (frg.cu:32).
- *   fpm            ntasks x 30 complex target parameters
+ *   fpm            ntasks x 30 complex target parameters (ntasks x np for a plug-in system)
  *   paths_per_task ntasks counts; total N = sum
- *   roots          out, N x 21 complex (canonical cognate, dehomogenized, frg.cu:59-68)
+ *   roots          out, N x 21 complex (canonical cognate, dehomogenized, frg.cu:59-68; a plug-in
+ *                  system's N x nv roots are dehomogenized as tracked)
  *   codes          out, N int32
- *   yfinal         optional out, N x 23 complex tracked endpoints before dehomogenizing
+ *   yfinal         optional out, N x 23 complex tracked endpoints before dehomogenizing (N x (nv + 2))
  *   resid          optional out, N doubles: max |F_r| / max_c |dF_r/dZ_c| at the root
  *   stats          optional out
  * Pointers may be host or device memory (probed). Synchronous. */

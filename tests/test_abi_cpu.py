@@ -1,5 +1,5 @@
 """The ctypes mirror of the C structs matches the header: sizes and field offsets of
-frg_config and frg_stats as the C compiler lays them out (CPU only)."""
+frg_config, frg_stats and frg_system_desc as the C compiler lays them out (CPU only)."""
 import ctypes
 import os
 import shutil
@@ -27,7 +27,8 @@ def _c_layout(tmp_path, struct, fields):
     return {k: int(v) for k, v in (ln.split() for ln in out.strip().splitlines())}
 
 
-@pytest.mark.parametrize("struct,cls", [("frg_config", frg.FrgConfig), ("frg_stats", frg.FrgStats)])
+@pytest.mark.parametrize("struct,cls", [("frg_config", frg.FrgConfig), ("frg_stats", frg.FrgStats),
+                                        ("frg_system_desc", frg.FrgSystemDesc)])
 def test_struct_layout_matches_header(tmp_path, struct, cls):
     names = [f for f, _ in cls._fields_]
     c = _c_layout(tmp_path, struct, names)
