@@ -95,4 +95,4 @@ def test_plugin_rounds_match_single_calls():
         for r, s in enumerate(seeds):
             single = t.track(task, [n], s)
             assert np.array_equal(codes[r * n:(r + 1) * n], single.codes)
-            assert np.array_equal(roots[r * n:(r + 1) * n], single.roots)
+            assert np.array_equal(roots[r * n:(r + 1) * n], single.roots, equal_nan=True)
