@@ -774,7 +774,7 @@ def run_plugin(args):
     distinct = []
     for j in range(T):
         sel = np.concatenate([np.arange(s * N + j * n, s * N + (j + 1) * n) for s in range(k)])
-        distinct.append(len(distinct_rows(r[sel], (c[sel] == 0) & (e[sel] <= RESID_MAX))))
+        distinct.append(len(distinct_rows(r[sel], (c[sel] == 0) & (e[sel] <= RESID_MAX), DUP_TOL, relative=True)))
     solves = st["ivp_solves"] + st["newton_iters"]
     fps = plugin_flops_per_solve(args.system, info.nv, info.np)
     peaks = measure_fma_peaks()

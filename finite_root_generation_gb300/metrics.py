@@ -29,11 +29,13 @@ def distinct_roots(roots, codes, resid=None, resid_max=1e-10, dup_tol=1e-6):
     return coll.roots()
 
 
-def distinct_rows(roots, keep=None, dup_tol=1e-6):
+def distinct_rows(roots, keep=None, dup_tol=1e-6, relative=False):
     """Distinct rows of `roots` ([n, nv] complex, any nv: the plug-in systems' roots),
     among those with `keep` true, by the collection's duplicate rule (every real
     component within dup_tol); the first of a group of duplicates in Re(root[0]) order
-    stays. Returns [k, nv] sorted by Re(root[0])."""
+    stays. Returns [k, nv] sorted by Re(root[0]). With `relative`, the tolerance of a
+    pair is dup_tol x max(1, the larger max-norm of the two), for roots large enough
+    that their last digits differ by more than dup_tol between paths."""
     r = np.asarray(roots, np.complex128)
     r = r.reshape(len(r), -1) if r.size else r.reshape(0, max(r.shape[-1] if r.ndim == 2 else 1, 1))
     if keep is not None:
@@ -41,13 +43,15 @@ def distinct_rows(roots, keep=None, dup_tol=1e-6):
     r = r[np.all(np.isfinite(r), axis=1)]
     r = r[np.argsort(r[:, 0].real, kind="stable")]
     parts = np.concatenate([r.real, r.imag], axis=1)
+    scale = np.maximum(1.0, np.max(np.abs(parts), axis=1)) if relative else np.ones(len(r))
+    window = dup_tol * (scale.max() if len(r) else 1.0)
     kept = []
     for i in range(len(r)):
         dup = False
         for j in reversed(kept):
-            if parts[i, 0] - parts[j, 0] > dup_tol:
+            if parts[i, 0] - parts[j, 0] > window:
                 break
-            if np.max(np.abs(parts[i] - parts[j])) <= dup_tol:
+            if np.max(np.abs(parts[i] - parts[j])) <= dup_tol * max(scale[i], scale[j]):
                 dup = True
                 break
         if not dup:

@@ -136,3 +136,14 @@ def test_capi_rejects_unsupported_plugin_configs_without_a_gpu():
         c = frg.default_config(**kw)
         assert lib.frg_track_noalloc(ctypes.byref(c), buf, 1, ppt, ctypes.c_uint64(1), buf, buf, None,
                                      None) == -1, kw
+
+
+def test_distinct_rows_relative_tolerance():
+    """Absolute tolerance keeps near copies of a large root apart; the relative option
+    merges them, and never merges distinct small roots."""
+    big = np.array([5e4 + 1j, 3.0, 2.0 - 1j])
+    rows = np.stack([big, big * (1 + 3e-11), big * (1 - 2e-11), np.array([0.1, 0.2, 0.3]),
+                     np.array([0.1 + 2e-6, 0.2, 0.3])])
+    assert len(distinct_rows(rows)) == 5
+    assert len(distinct_rows(rows, relative=True)) == 3
+    assert len(distinct_rows(rows, keep=[True, False, False, True, True], relative=True)) == 3
