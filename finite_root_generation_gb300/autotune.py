@@ -203,15 +203,19 @@ def _main(argv=None):
     ap.add_argument("--paths-per-task", type=int, default=4096)
     ap.add_argument("--rounds", type=int, default=8)
     ap.add_argument("--table", default=TUNED)
+    ap.add_argument("--space", default=None, help="search space as JSON (default: DEFAULT_SPACE)")
+    ap.add_argument("--target", type=float, default=0.995, help="recall target against plain FP64")
     args = ap.parse_args(argv)
+    space = json.loads(args.space) if args.space else None
     import torch
 
     tasks = np.stack([precision_point_task(k, "disk" if k % 2 == 0 else "curve") for k in range(8)])
     base = dict(start_dist=START_NORMAL, gamma_mode=GAMMA_RANDOM, inf_tol=1e-8, mixed_rounds=1, lo_endgame=1,
                 fp64_budget=10000, handback_good=32, fp64_segment=256, round_graph=1)
     seen = []
-    best = autotune(tasks, n=args.paths_per_task, rounds=args.rounds, base=base, cache=args.table + ".cache",
-                    retune=True, log=lambda e: (seen.append(e), print(json.dumps(e), flush=True)))
+    best = autotune(tasks, n=args.paths_per_task, rounds=args.rounds, base=base, space=space,
+                    target_recall=args.target, cache=args.table + ".cache", retune=True,
+                    log=lambda e: (seen.append(e), print(json.dumps(e), flush=True)))
     gpu = torch.cuda.get_device_name(0)
     table = {}
     if os.path.exists(args.table):
@@ -219,6 +223,7 @@ def _main(argv=None):
             table = json.load(f)
     table.setdefault(gpu, {})[args.workload] = {
         "best": best, "base": base, "paths_per_task": args.paths_per_task, "rounds": args.rounds,
+        "target_recall": args.target,
         "tasks": "seeds 0..7, unit disk / closed curve alternating", "candidates": seen}
     with open(args.table, "w") as f:
         json.dump(table, f, indent=1)
