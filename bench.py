@@ -763,18 +763,43 @@ def run_plugin(args):
         t0 = time.perf_counter()
         t.track_rounds(tasks, [n] * T, seeds, h_roots, h_codes, h_resid, depth=depth)
         e2e_s = time.perf_counter() - t0
+    # mixed precision on the same rounds: the thread kernel's FP32 stage with hand-off to FP64
+    mcfg = frg.plugin_config(args.system, precision=frg.PREC_MIXED, start_dist=frg.START_NORMAL,
+                             gamma_mode=frg.GAMMA_RANDOM, inf_tol=INF_TOL)
+    m_roots = torch.empty_like(roots)
+    m_codes = torch.empty_like(codes)
+    m_resid = torch.empty_like(resid)
+    with frg.Tracker(mcfg) as tm:
+        for w in range(args.warmup):
+            tm.track_rounds(fpm_d, [n] * T, [WARM_SEED_BASE + w], m_roots[:N], m_codes[:N], m_resid[:N], depth=1)
+        torch.cuda.synchronize()
+        st_m = tm.track_rounds(fpm_d, [n] * T, seeds, m_roots, m_codes, m_resid, depth=depth)
+        torch.cuda.synchronize()
     ms = st["track_ms"]
     r = roots.cpu().numpy().view(np.complex128).reshape(k * N, info.nv)
     c = codes.cpu().numpy()
     e = resid.cpu().numpy()
+    mr = m_roots.cpu().numpy().view(np.complex128).reshape(k * N, info.nv)
+    mc = m_codes.cpu().numpy()
+    me = m_resid.cpu().numpy()
     # the end-to-end run repeats the device run path for path (failed paths' non-finite
     # roots compare equal); reported, not asserted
     same = (c == h_codes) & np.all((r == h_roots) | (np.isnan(r) & np.isnan(h_roots)), axis=1)
     mismatch = int((~same).sum())
-    distinct = []
+    from finite_root_generation_gb300.metrics import recall
+
+    distinct, m_distinct = [], []
+    hits = total = 0
     for j in range(T):
         sel = np.concatenate([np.arange(s * N + j * n, s * N + (j + 1) * n) for s in range(k)])
-        distinct.append(len(distinct_rows(r[sel], (c[sel] == 0) & (e[sel] <= RESID_MAX), DUP_TOL, relative=True)))
+        a = distinct_rows(r[sel], (c[sel] == 0) & (e[sel] <= RESID_MAX), DUP_TOL, relative=True)
+        b = distinct_rows(mr[sel], (mc[sel] == 0) & (me[sel] <= RESID_MAX), DUP_TOL, relative=True)
+        distinct.append(len(a))
+        m_distinct.append(len(b))
+        hits += round(recall(a, b) * len(a))
+        total += len(a)
+    m_ms = st_m["track_ms"]
+    m_solves = st_m["ivp_solves"] + st_m["newton_iters"]
     solves = st["ivp_solves"] + st["newton_iters"]
     fps = plugin_flops_per_solve(args.system, info.nv, info.np)
     peaks = measure_fma_peaks()
@@ -798,7 +823,13 @@ def run_plugin(args):
                          "unit": "TFLOP/s", "frac": round(achieved / peaks["fp64"], 4), "traffic": None,
                          "flops_per_solve": fps, "solves": int(solves),
                          "peak_source": "of measured: bench.py's own FP64 FMA kernel"},
-            "gpu_launches": 3 * k, "clocks": clk.summary()}
+            "gpu_launches": 3 * k, "clocks": clk.summary(),
+            "mixed": {"value": round(k * N / (m_ms * 1e-3), 1), "unit": "paths/s",
+                      "speedup_vs_plain_fp64": round(ms / m_ms, 3), "recall_vs_plain_fp64": round(hits / max(total, 1), 5),
+                      "distinct_roots_per_task": {"min": min(m_distinct), "max": max(m_distinct)},
+                      "fp64_solve_share": round(st_m["fp64_solves"] / max(m_solves, 1), 4),
+                      "handoffs": int(st_m["handoffs"]),
+                      "codes": [int(x) for x in np.bincount(mc, minlength=8)]}}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle

@@ -197,10 +197,13 @@ def list_systems() -> list:
 
 
 def plugin_config(name: str, **overrides) -> FrgConfig:
-    """default_config for the plug-in system `name`: FP64 on the thread kernel."""
+    """default_config for the plug-in system `name` on the thread kernel (FP64 unless
+    `overrides` set precision=PREC_MIXED: the FP32 stage with hand-off to FP64)."""
     for s in list_systems():
         if s.name == name:
-            return default_config(system=s.id, precision=PREC_FP64, kernel_variant=KERNEL_THREAD, **overrides)
+            kw = dict(system=s.id, precision=PREC_FP64, kernel_variant=KERNEL_THREAD)
+            kw.update(overrides)
+            return default_config(**kw)
     raise FrgError(f"no system named {name}")
 
 

@@ -179,8 +179,8 @@ frg_status frg_check_config(frg_ctx* ctx, const frg_config* c) {
   if (c->precision == FRG_PREC_MIXED && !(c->newt_tol_lo > 0 && c->cond_switch > 1 && c->t_switch <= 1.0))
     return fail(ctx, FRG_ERR_ARG, "mixed precision needs newt_tol_lo > 0, cond_switch > 1, t_switch <= 1");
   if (c->system < 0 || c->system >= frg_num_systems()) return fail(ctx, FRG_ERR_ARG, "unknown system");
-  if (c->system != 0 && (c->precision != FRG_PREC_FP64 || c->kernel_variant != FRG_KERNEL_THREAD))
-    return fail(ctx, FRG_ERR_ARG, "plug-in systems run in FP64 on the thread kernel");
+  if (c->system != 0 && c->kernel_variant != FRG_KERNEL_THREAD)
+    return fail(ctx, FRG_ERR_ARG, "plug-in systems run on the thread kernel");
   return FRG_OK;
 }
 
@@ -382,12 +382,14 @@ static frg_status enqueue_track(frg_ctx* ctx, Slot& sl, const cx<double>* d_fpm,
   }
   // persistent grids: SMs x resident blocks, capped by the work (one path per thread
   // for the thread kernels, one per 8 lanes for the team kernels)
-  int plugin_bps = 0;  // a plug-in system's kernel has its own occupancy
-  if (ctx->cfg.system != 0) FRG_CUDA(ctx, frg_track_occupancy_system(ctx->cfg.system, &plugin_bps));
+  int plugin_bps[3] = {0, 0, 0};  // a plug-in system's kernels have their own occupancy
+  if (ctx->cfg.system != 0)
+    for (int m = 0; m < (mixed ? 3 : 1); ++m)
+      FRG_CUDA(ctx, frg_track_occupancy_system(ctx->cfg.system, m, &plugin_bps[m]));
   auto grid_for = [&](int mode, int64_t n) {
-    int bps = ctx->cfg.blocks_per_sm > 0 ? ctx->cfg.blocks_per_sm
-              : plugin_bps > 0           ? plugin_bps
-                                         : (team ? ctx->team_blocks_per_sm[mode] : ctx->blocks_per_sm[mode]);
+    int bps = ctx->cfg.blocks_per_sm > 0             ? ctx->cfg.blocks_per_sm
+              : (ctx->cfg.system != 0 && mode < 3)  ? plugin_bps[mode]
+                                                    : (team ? ctx->team_blocks_per_sm[mode] : ctx->blocks_per_sm[mode]);
     int64_t grid = (int64_t)ctx->sm_count * bps;
     int64_t per_block = team ? FRG_TEAM_THREADS / 8 : FRG_TRACK_THREADS;
     int64_t need = (n + per_block - 1) / per_block;

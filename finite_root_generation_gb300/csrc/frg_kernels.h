@@ -91,8 +91,9 @@ cudaError_t frg_launch_starts(const frg::TrackArgs& args, cx<double>* starts, cu
 cudaError_t frg_team_occupancy(int mode, int* blocks_per_sm);
 cudaError_t frg_launch_to_float(const cx<double>* in, cx<float>* out, int n, cudaStream_t stream);
 cudaError_t frg_launch_to_df(const cx<double>* in, cx<df>* out, int n, cudaStream_t stream);
-// Occupancy of the FP64 thread kernel of `system` (0 = Stephenson II, k = plug-in k).
-cudaError_t frg_track_occupancy_system(int system, int* blocks_per_sm);
+// Occupancy of the thread kernel of `system` (0 = Stephenson II, k = plug-in k) in `mode`
+// (0 plain FP64, 1 FP32 stage, 2 FP64 resume).
+cudaError_t frg_track_occupancy_system(int system, int mode, int* blocks_per_sm);
 // Name, unknowns and parameters of `system`; 0 for an unknown id. Host only.
 int frg_system_dims(int system, const char** name, int* nv, int* np);
 // Number of systems: Stephenson II and the generated plug-ins.

@@ -115,7 +115,7 @@ template <> __device__ __forceinline__ cx<float> task_gamma<float>(const TrackAr
 
 template <typename T, int NY_, int NP_>
 __device__ void save_handoff(const TrackArgs& a, const PathState<T, NY_, NP_>& P, int reason) {
-  static_assert(NY_ == NY, "hand-off records hold Stephenson II path states");
+  static_assert(NY_ <= NY, "hand-off records hold at most Stephenson II's 23-entry path states");
   Handoff& h = a.handoff[P.id];
 #pragma unroll 1
   for (int e = 0; e < NY_; ++e) {
@@ -477,11 +477,16 @@ cudaError_t launch(const frg::TrackArgs& args, int grid, cudaStream_t stream) {
 }  // namespace
 
 cudaError_t frg_launch_track(int mode, const frg::TrackArgs& args, int grid, cudaStream_t stream) {
-  if (args.cfg.system != 0) {  // plug-in systems: plain FP64 only
-    if (mode != frg::MODE_PLAIN) return cudaErrorInvalidValue;
+  if (args.cfg.system != 0) {  // plug-in systems: plain FP64, or the FP32 stage and the FP64 resume
     switch (args.cfg.system) {
-#define FRG_PLUGIN_LAUNCH(id, name, S) \
-  case id: return launch<frg::MODE_PLAIN, double, S>(args, grid, stream);
+#define FRG_PLUGIN_LAUNCH(id, name, S)                                                 \
+  case id:                                                                            \
+    switch (mode) {                                                                   \
+      case frg::MODE_PLAIN: return launch<frg::MODE_PLAIN, double, S>(args, grid, stream); \
+      case frg::MODE_LO: return launch<frg::MODE_LO, float, S>(args, grid, stream);         \
+      case frg::MODE_RESUME: return launch<frg::MODE_RESUME, double, S>(args, grid, stream); \
+      default: return cudaErrorInvalidValue;                                          \
+    }
       FRG_PLUGIN_LIST(FRG_PLUGIN_LAUNCH)
 #undef FRG_PLUGIN_LAUNCH
       default: return cudaErrorInvalidValue;
@@ -522,13 +527,23 @@ cudaError_t frg_track_occupancy(int mode, int* blocks_per_sm) {
   }
 }
 
-cudaError_t frg_track_occupancy_system(int system, int* blocks_per_sm) {
+template <int MODE, typename T, class S>
+static cudaError_t occ(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, frg::track_kernel<MODE, T, S>,
+                                                       FRG_TRACK_THREADS, 0);
+}
+
+cudaError_t frg_track_occupancy_system(int system, int mode, int* blocks_per_sm) {
+  if (system == 0) return frg_track_occupancy(mode, blocks_per_sm);
   switch (system) {
-    case 0: return frg_track_occupancy(frg::MODE_PLAIN, blocks_per_sm);
-#define FRG_PLUGIN_OCC(id, name, S)                                                                  \
-  case id:                                                                                          \
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                           \
-        blocks_per_sm, frg::track_kernel<frg::MODE_PLAIN, double, S>, FRG_TRACK_THREADS, 0);
+#define FRG_PLUGIN_OCC(id, name, S)                                             \
+  case id:                                                                     \
+    switch (mode) {                                                            \
+      case frg::MODE_PLAIN: return occ<frg::MODE_PLAIN, double, S>(blocks_per_sm); \
+      case frg::MODE_LO: return occ<frg::MODE_LO, float, S>(blocks_per_sm);         \
+      case frg::MODE_RESUME: return occ<frg::MODE_RESUME, double, S>(blocks_per_sm); \
+      default: return cudaErrorInvalidValue;                                   \
+    }
     FRG_PLUGIN_LIST(FRG_PLUGIN_OCC)
 #undef FRG_PLUGIN_OCC
     default: return cudaErrorInvalidValue;

@@ -125,8 +125,9 @@ typedef struct frg_config {
                             same results); 0 = launched one by one */
   int system;            /* the polynomial system tracked: 0 = Stephenson II (the reference's
                             htpykinematics.cu, nV = 21, nP = 30); k >= 1 = generated plug-in k
-                            (frg_system_info). A plug-in runs the FP64 thread kernel
-                            (precision FP64, kernel_variant THREAD) through frg_track,
+                            (frg_system_info). A plug-in runs on the thread kernel
+                            (kernel_variant THREAD), in FP64 or mixed precision (the FP32
+                            stage handing paths to FP64), through frg_track,
                             frg_track_async and frg_track_rounds; its tasks are ntasks x np
                             parameters, its roots N x nv, its yfinal N x (nv + 2), and its roots
                             are reported as tracked (no cognate map) */

@@ -15,7 +15,7 @@ import pytest
 
 import finite_root_generation_gb300 as frg
 from finite_root_generation_gb300 import build as frg_build
-from finite_root_generation_gb300.metrics import distinct_rows
+from finite_root_generation_gb300.metrics import distinct_rows, recall
 from finite_root_generation_gb300.systems import burmester5, conic2
 
 pytestmark = pytest.mark.gpu
@@ -96,3 +96,34 @@ def test_plugin_rounds_match_single_calls():
             single = t.track(task, [n], s)
             assert np.array_equal(codes[r * n:(r + 1) * n], single.codes)
             assert np.array_equal(roots[r * n:(r + 1) * n], single.roots, equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["conic2", "burmester5"])
+def test_plugin_mixed_precision_finds_the_plain_roots(name):
+    """Mixed precision on a plug-in (the thread kernel's FP32 stage handing ill-conditioned
+    steps, the endgame and the finish to FP64) finds every distinct finite root plain FP64
+    finds on the same paths, each with residual <= 1e-10 (at most 1e-3 of the successes
+    filtered)."""
+    if name == "conic2":
+        rng = np.random.default_rng(31)
+        tasks = np.stack([conic2.line_pair_task(rng.normal(size=4) + 1j * rng.normal(size=4),
+                                                rng.normal(size=4) + 1j * rng.normal(size=4))[0] for _ in range(2)])
+    else:
+        tasks = np.stack([burmester5.physical_task(np.random.default_rng(s)) for s in (11, 12)])
+    n = 2048
+    kw = dict(start_dist=frg.START_NORMAL, gamma_mode=frg.GAMMA_RANDOM, inf_tol=INF_TOL)
+    with frg.Tracker(frg.plugin_config(name, **kw)) as t:
+        plain = t.track(tasks, [n, n], 23, want_resid=True)
+    with frg.Tracker(frg.plugin_config(name, precision=frg.PREC_MIXED, **kw)) as t:
+        mixed = t.track(tasks, [n, n], 23, want_resid=True)
+    ok = mixed.codes == 0
+    bad = int(np.sum(~(mixed.resid[ok] <= 1e-10)))
+    print(f"{name} mixed: codes {np.bincount(mixed.codes, minlength=8)}, {mixed.stats['handoffs']} hand-offs, "
+          f"{bad} above the residual bar, track {mixed.stats['track_ms']:.1f} ms vs plain "
+          f"{plain.stats['track_ms']:.1f} ms")
+    assert bad <= 1e-3 * ok.sum() + 1
+    for k in range(2):
+        sl = slice(k * n, (k + 1) * n)
+        a = distinct_rows(plain.roots[sl], (plain.codes[sl] == 0) & (plain.resid[sl] <= 1e-10), relative=True)
+        b = distinct_rows(mixed.roots[sl], (mixed.codes[sl] == 0) & (mixed.resid[sl] <= 1e-10), relative=True)
+        assert len(a) == 4 and recall(a, b) == 1.0, (len(a), len(b))
