@@ -14,7 +14,9 @@
 // around it diverges. The decisions, tolerances, counters and random draws are the
 // reference's, so a path ends with the reference's code and root.
 //
-// Three instantiations:
+// Three modes, each instantiated for Stephenson II (SysStephenson2) and for every
+// generated plug-in system (frg_plugins_gen.cuh), whose sizes set the path state and
+// the dense system:
 //   MODE_PLAIN   FP64 throughout, from the start system to the root (the reference's
 //                arithmetic);
 //   MODE_LO      FP32 state and linear algebra from the start system; a path is handed
