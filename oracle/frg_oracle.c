@@ -9,6 +9,11 @@
  * tests pin them against golden vectors recorded from the reference itself.
  *
  * Complex division is Smith's algorithm (R. L. Smith, CACM 5(8), 1962).
+ *
+ * The tracker (IVP, DP6(5), Newton, TrackPath) takes the system as a parameter (osys):
+ * Stephenson II, restated here, or a generated plug-in system (frg_plugins_gen.h, from the
+ * sympy modules in finite_root_generation_gb300/systems), which has no reference
+ * counterpart; its rows are checked against the symbolic system in tests/.
  */
 #define _GNU_SOURCE
 #include "frg_oracle.h"
