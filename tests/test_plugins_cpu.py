@@ -16,9 +16,10 @@ import pytest
 
 import finite_root_generation_gb300 as frg
 from finite_root_generation_gb300.metrics import distinct_rows
-from finite_root_generation_gb300.systems import PLUGINS, burmester5, conic2
 
-sp = pytest.importorskip("sympy")
+sp = pytest.importorskip("sympy")  # the plug-in modules state their systems in sympy
+
+from finite_root_generation_gb300.systems import PLUGINS, burmester5, conic2  # noqa: E402
 
 MODULES = {"conic2": conic2, "burmester5": burmester5}
 
