@@ -148,3 +148,29 @@ def test_distinct_rows_relative_tolerance():
     assert len(distinct_rows(rows)) == 5
     assert len(distinct_rows(rows, relative=True)) == 3
     assert len(distinct_rows(rows, keep=[True, False, False, True, True], relative=True)) == 3
+
+
+def test_generator_rejects_malformed_systems():
+    """A plug-in needs one polynomial equation per unknown and one solved parameter per
+    equation in which the system is linear."""
+    import types
+
+    from finite_root_generation_gb300.gen import gen_plugins
+
+    x, y, a, b, c = sp.symbols("x y a b c")
+
+    def spec(eqs, solved, unknowns=(x, y), params=(a, b, c)):
+        return types.SimpleNamespace(NAME="bad", UNKNOWNS=list(unknowns), PARAMS=list(params), EQUATIONS=eqs,
+                                     SOLVED=solved)
+
+    good = spec([a * x**2 + y - b, x * y - c], [b, c])
+    info = gen_plugins.analyse(good)
+    assert (info["nv"], info["np"], info["ns"]) == (2, 3, 2)
+    with pytest.raises(ValueError, match="one equation per unknown"):
+        gen_plugins.analyse(spec([x - a], [a]))
+    with pytest.raises(ValueError, match="SOLVED"):
+        gen_plugins.analyse(spec([x - a, y - b], [a]))
+    with pytest.raises(ValueError, match="linear in SOLVED"):
+        gen_plugins.analyse(spec([x - b**2, y - c], [b, c]))
+    with pytest.raises(sp.PolynomialError):
+        gen_plugins.analyse(spec([x - 1 / y + b, y - c], [b, c]))
