@@ -279,7 +279,9 @@ frg_status frg_track_noalloc(const frg_config* cfg, const double* fpm, int ntask
                              uint64_t seed, double* roots, int32_t* codes, double* resid, void* stream);
 
 /* ---- root collection (replaces SortingDeletingMerging, frgsupport.cu:10-215, and
- *      the thrust ordering of frg.cu:432-435) ---- */
+ *      the thrust ordering of frg.cu:432-435). The host and device collections hold
+ *      Stephenson II roots (21 complex, the fptColl layout); a plug-in system's roots
+ *      are deduplicated by the caller. ---- */
 typedef struct frg_coll frg_coll;
 
 frg_status frg_coll_create(frg_coll** coll, double dup_tol);
